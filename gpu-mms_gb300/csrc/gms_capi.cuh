@@ -1,0 +1,63 @@
+// Shared plumbing of the C ABI (include/gms.h): status/error recording, the
+// per-(device, stream) scratch cache, and the engine instantiations used by
+// the prebuilt dtypes.
+#pragma once
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+
+#include "../../include/gms.h"
+#include "gms_sort.cuh"
+
+namespace gms_capi {
+
+// Engines of the prebuilt dtypes.  32-bit keys and 64-bit keys share one
+// geometry: 512 threads x 17 keys = 8704-key tiles (17 is odd, so the
+// thread-strided shared-memory accesses of a warp fall in distinct banks).
+constexpr int kNT = 512;
+constexpr int kItems = 17;
+
+template <class K, class Codec>
+using KeysEngine = gms::Engine<K, gms::NoVal, gms::KeyLess, Codec, false, kNT, kItems>;
+template <class K, class Codec>
+using KvEngine = gms::Engine<K, int32_t, gms::KeyLess, Codec, true, kNT, kItems>;
+
+// error recording (defined in gms_capi_misc.cu)
+int set_error(int status, const char* msg);
+int cuda_error(cudaError_t e, const char* where);
+void clear_error();
+
+// Scratch cache.  `tag` separates independent buffers of one call.
+void* cache_get(int tag, size_t bytes, cudaStream_t st, int* status);
+
+inline gms::Tune default_tune() { return gms::Tune{}; }
+
+// Runs a full sort of one dtype with the scratch cache.
+template <class Eng, class K, class V>
+int run_sort(K* in, V* vin, K* out, V* vout, int64_t n, cudaStream_t st) {
+  clear_error();
+  if (n < 0) return set_error(GMS_ERR_INVALID, "n < 0");
+  if (n == 0) return GMS_OK;
+  if (!in || !out) return set_error(GMS_ERR_INVALID, "null key pointer");
+  if (gms::HasVal<V>::value && (!vin || !vout)) return set_error(GMS_ERR_INVALID, "null value pointer");
+  if (n > ((int64_t)1 << 32) * 32) return set_error(GMS_ERR_TOO_LARGE, "n beyond 2^37");
+  const gms::Tune t = default_tune();
+  const gms::WsLayout l = Eng::plan(n, t);
+  const size_t bytes = gms::ws_bytes_for<K>(l, t.k);
+  int status = GMS_OK;
+  void* ws = cache_get(0, bytes, st, &status);
+  if (status != GMS_OK) return status;
+  const gms::WsPtrs<K> w = gms::ws_carve<K>(l, t.k, ws);
+  cudaError_t e = Eng::sort(w, in, vin, out, vout, n, t, st);
+  if (e != cudaSuccess) return cuda_error(e, "sort");
+  return GMS_OK;
+}
+
+template <class Eng, class K>
+size_t sort_ws_bytes(int64_t n) {
+  const gms::Tune t = default_tune();
+  return gms::ws_bytes_for<K>(Eng::plan(n, t), t.k);
+}
+
+}  // namespace gms_capi

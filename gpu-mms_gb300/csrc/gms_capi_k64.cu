@@ -1,0 +1,60 @@
+// C ABI: 64-bit keys (int64, uint64, float64), keys only.
+#include "gms_capi.cuh"
+
+using namespace gms_capi;
+using gms::NoVal;
+
+namespace {
+
+using EngI64 = KeysEngine<uint64_t, gms::SignFlip64>;
+using EngU64 = KeysEngine<uint64_t, gms::IdentityCodec<uint64_t>>;
+using EngF64 = KeysEngine<uint64_t, gms::FloatOrder64>;
+
+template <class Eng>
+int sort64(void* in, void* out, int64_t n, void* st) {
+  return run_sort<Eng, uint64_t, NoVal>((uint64_t*)in, nullptr, (uint64_t*)out, nullptr, n, (cudaStream_t)st);
+}
+
+}  // namespace
+
+extern "C" {
+
+int gms_sort_i64(int64_t* in, int64_t* out, int64_t n, int tb, void* st) {
+  (void)tb;
+  return sort64<EngI64>(in, out, n, st);
+}
+int gms_sort_u64(uint64_t* in, uint64_t* out, int64_t n, int tb, void* st) {
+  (void)tb;
+  return sort64<EngU64>(in, out, n, st);
+}
+int gms_sort_f64(double* in, double* out, int64_t n, int tb, void* st) {
+  (void)tb;
+  return sort64<EngF64>(in, out, n, st);
+}
+
+int gms_tile_sort_u64(uint64_t* data, int64_t n, int64_t tile, void* st) {
+  clear_error();
+  if (n < 0 || tile < 1 || tile > EngU64::CAP) return set_error(GMS_ERR_INVALID, "bad n or tile");
+  if (n == 0) return GMS_OK;
+  if (!data) return set_error(GMS_ERR_INVALID, "null pointer");
+  cudaError_t e = EngU64::tile_sort(data, n, tile, (cudaStream_t)st);
+  return e == cudaSuccess ? GMS_OK : cuda_error(e, "tile_sort");
+}
+
+int gms_merge_level_u64(const uint64_t* in, uint64_t* out, int64_t n, int64_t run_len, int k, void* st) {
+  clear_error();
+  if (n < 0 || run_len < 1 || k < 2 || k > 32) return set_error(GMS_ERR_INVALID, "bad n, run_len or k");
+  if (n == 0) return GMS_OK;
+  if (!in || !out) return set_error(GMS_ERR_INVALID, "null pointer");
+  gms::Tune t = default_tune();
+  t.k = k;
+  const gms::WsLayout l = EngU64::plan_merge_level(n, run_len, t);
+  int status = GMS_OK;
+  void* ws = cache_get(0, gms::ws_bytes_for<uint64_t>(l, k), (cudaStream_t)st, &status);
+  if (status != GMS_OK) return status;
+  const gms::WsPtrs<uint64_t> w = gms::ws_carve<uint64_t>(l, k, ws);
+  cudaError_t e = EngU64::merge_level(w, in, out, n, run_len, t, (cudaStream_t)st);
+  return e == cudaSuccess ? GMS_OK : cuda_error(e, "merge_level");
+}
+
+}  // extern "C"

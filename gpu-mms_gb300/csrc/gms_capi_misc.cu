@@ -1,0 +1,164 @@
+// C ABI: version, status strings, error recording, scratch cache, queries.
+#include <mutex>
+#include <vector>
+
+#include "gms_capi.cuh"
+
+namespace gms_capi {
+
+static thread_local std::string g_last_error;
+
+int set_error(int status, const char* msg) {
+  g_last_error = msg ? msg : "";
+  return status;
+}
+int cuda_error(cudaError_t e, const char* where) {
+  char buf[256];
+  snprintf(buf, sizeof(buf), "%s: %s (%s)", where, cudaGetErrorString(e), cudaGetErrorName(e));
+  g_last_error = buf;
+  return e == cudaErrorMemoryAllocation ? GMS_ERR_NOMEM : GMS_ERR_CUDA;
+}
+void clear_error() { g_last_error.clear(); }
+
+namespace {
+struct Slot {
+  int dev;
+  cudaStream_t stream;
+  int tag;
+  void* ptr;
+  size_t bytes;
+};
+std::mutex g_mu;
+std::vector<Slot> g_slots;
+}  // namespace
+
+void* cache_get(int tag, size_t bytes, cudaStream_t st, int* status) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) {
+    *status = cuda_error(e, "cudaGetDevice");
+    return nullptr;
+  }
+  std::lock_guard<std::mutex> g(g_mu);
+  for (Slot& s : g_slots) {
+    if (s.dev == dev && s.stream == st && s.tag == tag) {
+      if (s.bytes >= bytes) return s.ptr;
+      // grow: the previous call on this stream may still use the buffer
+      e = cudaStreamSynchronize(st);
+      if (e != cudaSuccess) {
+        *status = cuda_error(e, "cudaStreamSynchronize");
+        return nullptr;
+      }
+      cudaFree(s.ptr);
+      s.ptr = nullptr;
+      s.bytes = 0;
+      e = cudaMalloc(&s.ptr, bytes);
+      if (e != cudaSuccess) {
+        s.ptr = nullptr;
+        *status = cuda_error(e, "cudaMalloc(scratch)");
+        return nullptr;
+      }
+      s.bytes = bytes;
+      cudaMemset(s.ptr, 0, bytes < 256 ? bytes : 256);  // status word starts clear
+      return s.ptr;
+    }
+  }
+  void* p = nullptr;
+  e = cudaMalloc(&p, bytes > 0 ? bytes : 256);
+  if (e != cudaSuccess) {
+    *status = cuda_error(e, "cudaMalloc(scratch)");
+    return nullptr;
+  }
+  cudaMemset(p, 0, 256);  // status word starts clear
+  g_slots.push_back(Slot{dev, st, tag, p, bytes > 0 ? bytes : 256});
+  return p;
+}
+
+}  // namespace gms_capi
+
+using namespace gms_capi;
+
+extern "C" {
+
+int gms_version(void) { return 100; }
+
+const char* gms_status_string(int s) {
+  switch (s) {
+    case GMS_OK: return "GMS_OK";
+    case GMS_ERR_INVALID: return "GMS_ERR_INVALID";
+    case GMS_ERR_CUDA: return "GMS_ERR_CUDA";
+    case GMS_ERR_NOMEM: return "GMS_ERR_NOMEM";
+    case GMS_ERR_TOO_LARGE: return "GMS_ERR_TOO_LARGE";
+    case GMS_ERR_INTERNAL: return "GMS_ERR_INTERNAL";
+    default: return "GMS_ERR_UNKNOWN";
+  }
+}
+
+const char* gms_last_error(void) { return g_last_error.c_str(); }
+
+void gms_release_workspaces(void) {
+  std::lock_guard<std::mutex> g(g_mu);
+  for (Slot& s : g_slots) {
+    int cur = 0;
+    cudaGetDevice(&cur);
+    cudaSetDevice(s.dev);
+    cudaFree(s.ptr);
+    cudaSetDevice(cur);
+  }
+  g_slots.clear();
+}
+
+int64_t gms_max_tile(void) { return (int64_t)kNT * kItems; }
+
+int64_t gms_base_tile(int dtype, int kv) {
+  (void)dtype;
+  (void)kv;
+  return (int64_t)kNT * kItems;
+}
+
+int gms_rounds(int dtype, int kv, int64_t n) {
+  (void)dtype;
+  (void)kv;
+  int p = 0;
+  for (int64_t L = (int64_t)kNT * kItems; L < n; L *= default_tune().k) ++p;
+  return p;
+}
+
+size_t gms_workspace_bytes(int dtype, int kv, int64_t n) {
+  if (n <= 0) return 0;
+  const bool wide = (dtype >= 3);
+  if (wide) {
+    return kv ? sort_ws_bytes<KvEngine<uint64_t, gms::IdentityCodec<uint64_t>>, uint64_t>(n)
+              : sort_ws_bytes<KeysEngine<uint64_t, gms::IdentityCodec<uint64_t>>, uint64_t>(n);
+  }
+  return kv ? sort_ws_bytes<KvEngine<uint32_t, gms::IdentityCodec<uint32_t>>, uint32_t>(n)
+            : sort_ws_bytes<KeysEngine<uint32_t, gms::IdentityCodec<uint32_t>>, uint32_t>(n);
+}
+
+int gms_device_status(void* stream, int* status_out) {
+  clear_error();
+  if (!status_out) return set_error(GMS_ERR_INVALID, "null status_out");
+  *status_out = 0;
+  cudaStream_t st = (cudaStream_t)stream;
+  int status = GMS_OK;
+  void* ws = cache_get(0, 256, st, &status);
+  if (status != GMS_OK) return status;
+  cudaError_t e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_error(e, "cudaStreamSynchronize");
+  int v = 0;
+  e = cudaMemcpy(&v, ws, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemset(ws, 0, sizeof(int));
+  if (e != cudaSuccess) return cuda_error(e, "status word");
+  *status_out = v;
+  return GMS_OK;
+}
+
+int gms_reserve(int dtype, int kv, int64_t n, void* stream) {
+  clear_error();
+  if (dtype < 0 || dtype > 5 || n < 0) return set_error(GMS_ERR_INVALID, "bad dtype or n");
+  int status = GMS_OK;
+  cache_get(0, gms_workspace_bytes(dtype, kv, n), (cudaStream_t)stream, &status);
+  return status;
+}
+
+}  // extern "C"

@@ -1,0 +1,306 @@
+// Device building blocks of the GB300 multiway mergesort.
+//
+// Reference counterparts (GPU-MMS, paths relative to its src/):
+//   cmpSwap / swap* / myMin / myMax        basecase/util.hxx:39-215
+//   bitonicSort32 (register network)       basecase/sortRowMajor.hxx:96-119
+//   shfl_wrapper / SHFL_XOR                basecase/sortRowMajor.hxx:36-42, params.h:40-50
+//   xorMergeNodes / xorMergeGeneral        io-merge-gen.hxx:48-93, 204-236
+//
+// The reference merges 32-key heap nodes with warp-shuffle bitonic networks.
+// Here a merge step is a merge-path split (binary search on one diagonal)
+// followed by a branch-free serial merge of ITEMS keys per thread out of shared
+// memory: about log2(K) comparisons per key per K-way round instead of a
+// bitonic network per heap level.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace gms {
+
+// ---------------------------------------------------------------------------
+// Payload marker for keys-only sorts.
+struct NoVal {};
+
+template <class V>
+struct HasVal {
+  static constexpr bool value = true;
+};
+template <>
+struct HasVal<NoVal> {
+  static constexpr bool value = false;
+};
+
+// ---------------------------------------------------------------------------
+// Codecs map a user key's bit pattern to an unsigned key whose `<` order is
+// the user order, and back.  The first pass encodes on load, the last pass
+// decodes on store; every pass in between compares plain unsigned integers.
+template <class K>
+struct IdentityCodec {
+  static __device__ __forceinline__ K enc(K x) { return x; }
+  static __device__ __forceinline__ K dec(K x) { return x; }
+};
+// two's-complement order -> unsigned order
+struct SignFlip32 {
+  static __device__ __forceinline__ uint32_t enc(uint32_t x) { return x ^ 0x80000000u; }
+  static __device__ __forceinline__ uint32_t dec(uint32_t x) { return x ^ 0x80000000u; }
+};
+struct SignFlip64 {
+  static __device__ __forceinline__ uint64_t enc(uint64_t x) { return x ^ 0x8000000000000000ull; }
+  static __device__ __forceinline__ uint64_t dec(uint64_t x) { return x ^ 0x8000000000000000ull; }
+};
+// IEEE-754 totalOrder over bit patterns: -NaN < -Inf < ... < -0 < +0 < ... < +Inf < +NaN
+struct FloatOrder32 {
+  static __device__ __forceinline__ uint32_t enc(uint32_t b) {
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+  }
+  static __device__ __forceinline__ uint32_t dec(uint32_t k) {
+    return (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
+  }
+};
+struct FloatOrder64 {
+  static __device__ __forceinline__ uint64_t enc(uint64_t b) {
+    return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+  }
+  static __device__ __forceinline__ uint64_t dec(uint64_t k) {
+    return (k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k;
+  }
+};
+
+// Default strict weak order on the stored keys.
+struct KeyLess {
+  template <class K>
+  __device__ __forceinline__ bool operator()(const K& a, const K& b) const {
+    return a < b;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Register sorting networks.  Indices are compile-time after unrolling, so the
+// keys stay in registers (no local memory).
+
+// Compare-exchange: afterwards a <= b.  Not stable (used where equivalent keys
+// are bit-identical).
+template <class K, class Cmp>
+__device__ __forceinline__ void cas(K& a, K& b, Cmp cmp) {
+  const bool sw = cmp(b, a);
+  const K lo = sw ? b : a;
+  const K hi = sw ? a : b;
+  a = lo;
+  b = hi;
+}
+
+// Batcher odd-even merge sort for N keys, pruned from the next power of two.
+// A comparator whose upper index is >= N only ever meets a virtual +inf there
+// and is dropped.  The comparator list is built at compile time and expanded
+// by template recursion, so every index is a constant.
+struct NetTable {
+  int a[1024];
+  int b[1024];
+  int n;
+};
+
+constexpr NetTable batcher_table(int N) {
+  NetTable t{};
+  t.n = 0;
+  int P = 1;
+  while (P < N) P *= 2;
+  for (int p = 1; p < P; p *= 2) {
+    for (int k = p; k >= 1; k /= 2) {
+      for (int j = k % p; j + k < P; j += 2 * k) {
+        for (int i = 0; i < k; ++i) {
+          if (i + j + k < N && (i + j) / (2 * p) == (i + j + k) / (2 * p)) {
+            t.a[t.n] = i + j;
+            t.b[t.n] = i + j + k;
+            ++t.n;
+          }
+        }
+      }
+    }
+  }
+  return t;
+}
+
+template <int N>
+struct Batcher {
+  static constexpr NetTable table = batcher_table(N);
+};
+
+template <int N, int C, class K, class Cmp>
+__device__ __forceinline__ void network_apply(K (&r)[N], Cmp cmp) {
+  if constexpr (C < Batcher<N>::table.n) {
+    constexpr int ia = Batcher<N>::table.a[C];
+    constexpr int ib = Batcher<N>::table.b[C];
+    cas(r[ia], r[ib], cmp);
+    network_apply<N, C + 1>(r, cmp);
+  }
+}
+
+template <int N, class K, class Cmp>
+__device__ __forceinline__ void network_sort(K (&r)[N], Cmp cmp) {
+  network_apply<N, 0>(r, cmp);
+}
+
+// Odd-even transposition sort: only adjacent keys are exchanged, and only when
+// strictly out of order, so equal keys keep their order (stable).  Carries a
+// payload along.
+template <int N, class K, class V, class Cmp>
+__device__ __forceinline__ void transposition_sort(K (&r)[N], V (&v)[N], Cmp cmp) {
+#pragma unroll
+  for (int round = 0; round < N; ++round) {
+#pragma unroll
+    for (int i = round & 1; i + 1 < N; i += 2) {
+      const bool sw = cmp(r[i + 1], r[i]);
+      const K klo = sw ? r[i + 1] : r[i];
+      const K khi = sw ? r[i] : r[i + 1];
+      r[i] = klo;
+      r[i + 1] = khi;
+      if constexpr (HasVal<V>::value) {
+        const V vlo = sw ? v[i + 1] : v[i];
+        const V vhi = sw ? v[i] : v[i + 1];
+        v[i] = vlo;
+        v[i + 1] = vhi;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Merge path: number of elements of `a` among the first `diag` outputs of the
+// stable merge of a and b (a wins ties).
+template <class K, class Cmp>
+__device__ __forceinline__ int merge_path(const K* a, int na, const K* b, int nb, int diag, Cmp cmp) {
+  int lo = diag - nb > 0 ? diag - nb : 0;
+  int hi = diag < na ? diag : na;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (!cmp(b[diag - 1 - mid], a[mid])) {
+      lo = mid + 1;
+    } else {
+      hi = mid;
+    }
+  }
+  return lo;
+}
+
+// One level of pairwise merging over runs of equal length `rl` inside a
+// shared-memory tile of `cap` keys (cap a multiple of 2*rl or the tail run
+// shorter).  Thread `t` produces outputs [t*ITEMS, t*ITEMS + ITEMS) into
+// registers.  ITEMS divides rl, so a thread never straddles two pairs.
+template <int ITEMS, class K, class V, class Cmp>
+__device__ __forceinline__ void merge_level_regular(const K* sk, const V* sv, int cap, int rl, int s,
+                                                    K (&ok)[ITEMS], V (&ov)[ITEMS], Cmp cmp) {
+  const int ps = (s / (2 * rl)) * (2 * rl);
+  const int pm = min(ps + rl, cap);
+  const int pe = min(ps + 2 * rl, cap);
+  const int diag = s - ps;
+  const int ia = merge_path(sk + ps, pm - ps, sk + pm, pe - pm, diag, cmp);
+  int xa = ps + ia;
+  int xb = pm + (diag - ia);
+  K ka = sk[xa];
+  K kb = sk[xb];
+#pragma unroll
+  for (int i = 0; i < ITEMS; ++i) {
+    const bool ta = (xb >= pe) || ((xa < pm) && !cmp(kb, ka));
+    ok[i] = ta ? ka : kb;
+    if constexpr (HasVal<V>::value) ov[i] = sv[ta ? xa : xb];
+    if (ta) {
+      ++xa;
+      ka = sk[xa];
+    } else {
+      ++xb;
+      kb = sk[xb];
+    }
+  }
+}
+
+// One level of pairwise merging over K variable-length runs whose boundaries
+// are pre[0..K] (pre[K] = total).  At level `span` (2, 4, 8, ...) the runs
+// [pre[p*span], pre[p*span+span/2]) and [pre[p*span+span/2], pre[p*span+span])
+// are merged.  Runs may be empty; a thread whose ITEMS outputs straddle the end
+// of one pair continues with the next non-empty pair.
+template <int ITEMS, class K, class V, class Cmp>
+__device__ __forceinline__ void merge_level_var(const K* sk, const V* sv, const int* pre, int nk, int span,
+                                                int s, int e, K (&ok)[ITEMS], V (&ov)[ITEMS], Cmp cmp) {
+  const int npairs = (nk + span - 1) / span;
+  // largest pair index whose start is <= s
+  int lo = 0, hi = npairs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (pre[mid * span] <= s) {
+      lo = mid;
+    } else {
+      hi = mid - 1;
+    }
+  }
+  int p = lo;
+  int ps = pre[p * span];
+  int pm = pre[min(p * span + span / 2, nk)];
+  int pe = pre[min(p * span + span, nk)];
+  const int diag = s - ps;
+  const int ia = merge_path(sk + ps, pm - ps, sk + pm, pe - pm, diag, cmp);
+  int xa = ps + ia;
+  int xb = pm + (diag - ia);
+  K ka = sk[xa];
+  K kb = sk[xb];
+#pragma unroll
+  for (int i = 0; i < ITEMS; ++i) {
+    if (s + i < e) {
+      if (xa >= pm && xb >= pe) {
+        // pair exhausted at position s+i == pe: move to the pair that holds it
+        const int q = s + i;
+        int l2 = p + 1, h2 = npairs - 1;
+        while (l2 < h2) {
+          const int mid = (l2 + h2 + 1) >> 1;
+          if (pre[mid * span] <= q) {
+            l2 = mid;
+          } else {
+            h2 = mid - 1;
+          }
+        }
+        p = l2 < npairs - 1 ? l2 : npairs - 1;
+        ps = pre[p * span];
+        pm = pre[min(p * span + span / 2, nk)];
+        pe = pre[min(p * span + span, nk)];
+        xa = ps;
+        xb = pm;
+        ka = sk[xa];
+        kb = sk[xb];
+      }
+      const bool ta = (xb >= pe) || ((xa < pm) && !cmp(kb, ka));
+      ok[i] = ta ? ka : kb;
+      if constexpr (HasVal<V>::value) ov[i] = sv[ta ? xa : xb];
+      if (ta) {
+        ++xa;
+        ka = sk[xa];
+      } else {
+        ++xb;
+        kb = sk[xb];
+      }
+    }
+  }
+}
+
+// Largest element (under cmp) across the block; every thread gets it.
+// `scratch` holds NT keys.  Shared-memory tree, so any copyable key type works
+// (no shuffle of user types).
+template <int NT, class K, class Cmp>
+__device__ __forceinline__ K block_max(K x, K* scratch, Cmp cmp) {
+  const int t = threadIdx.x;
+  scratch[t] = x;
+  __syncthreads();
+#pragma unroll
+  for (int s = NT / 2; s > 0; s >>= 1) {
+    if (t < s) {
+      const K a = scratch[t];
+      const K b = scratch[t + s];
+      scratch[t] = cmp(a, b) ? b : a;
+    }
+    __syncthreads();
+  }
+  const K m = scratch[0];
+  __syncthreads();
+  return m;
+}
+
+}  // namespace gms

@@ -1,0 +1,437 @@
+// Kernels of one multiway-mergesort round on GB300 (sm_103a).
+//
+// Reference counterparts (GPU-MMS, paths relative to its src/):
+//   squareSort            basecase/squareSort.hxx:62-131   -> tile_kernel<MODE_BASE>
+//   multimergeLevel       multimergesort.hxx:155-209       -> tile_kernel<MODE_GROUP / MODE_TILE>
+//   multimergePipeline    io-merge-gen.hxx:306-355         -> the shared-memory merge levels
+//   findPartitions        warp-partition.hxx:488-532       -> splitter_kernel
+//   pad                   pad.hxx:1-4                      -> in-kernel tail padding (MODE_BASE)
+//
+// Layout: one CTA owns one tile of at most CAP = NT*ITEMS keys (+ payload) in
+// shared memory.  A tile is loaded with coalesced loads, merged in
+// ceil(log2 K) pairwise merge-path levels (results pass through registers and
+// back to the same buffer), and stored with coalesced stores.  While storing,
+// the CTA also writes every B-th key of its output run (the block sample the
+// next round uses to cut its tiles).
+#pragma once
+
+#include "gms_device.cuh"
+
+namespace gms {
+
+enum TileMode : int { MODE_BASE = 0, MODE_GROUP = 1, MODE_TILE = 2 };
+
+// Arguments of one launch of tile_kernel.
+template <class K, class V>
+struct TileArgs {
+  const K* in;
+  K* out;
+  const V* vin;
+  V* vout;
+  int64_t n;      // elements in the array
+  int64_t L;      // input run length (GROUP/TILE); tile length (BASE)
+  int k;          // fan-in: runs per group (GROUP/TILE)
+  // MODE_TILE: tile boundaries.  Row r of `desc` holds the run-relative start
+  // of every run of the group; `doff[r]` is the group-relative output offset.
+  const int64_t* desc;
+  const int64_t* doff;
+  int64_t tiles_full;  // tiles of a full group
+  int64_t tiles_last;  // tiles of the last group
+  int64_t groups;
+  // block sample of the output runs (for the next round); null if unused
+  K* sample_out;
+  int64_t out_run_len;     // length of an output run
+  int64_t sample_run_len;  // ceil(out_run_len / sample_b)
+  int sample_b;
+  int enc_on_load;   // apply Codec::enc to loaded keys
+  int dec_on_store;  // apply Codec::dec to stored keys
+  int gen_index;     // payload = input position (uint32), ignoring vin
+  int* err;          // device status word (bit 0: tile over capacity); may be null
+};
+
+// Bits of the device status word.
+enum DeviceStatus : int { DEV_TILE_OVERFLOW = 1, DEV_BAD_SEGMENT = 2 };
+
+template <class K, class V, int CAP>
+struct TileSmemLayout {
+  static constexpr bool kHasVal = HasVal<V>::value;
+  static constexpr size_t key_bytes = ((sizeof(K) * (CAP + 1) + 15) / 16) * 16;
+  static constexpr size_t val_bytes = kHasVal ? ((sizeof(V) * (CAP + 1) + 15) / 16) * 16 : 0;
+  static constexpr int kMaxK = 32;
+  static constexpr size_t pre_bytes = 16 * ((sizeof(int) * (kMaxK + 1) + 15) / 16);
+  static constexpr size_t gs_bytes = sizeof(int64_t) * kMaxK;
+  static constexpr size_t bytes = key_bytes + val_bytes + pre_bytes + gs_bytes;
+};
+
+__device__ __forceinline__ int64_t min64(int64_t a, int64_t b) { return a < b ? a : b; }
+
+template <class Codec, class K>
+__device__ __forceinline__ K maybe_enc(K x, int on) {
+  return on ? Codec::enc(x) : x;
+}
+template <class Codec, class K>
+__device__ __forceinline__ K maybe_dec(K x, int on) {
+  return on ? Codec::dec(x) : x;
+}
+
+// ---------------------------------------------------------------------------
+// The tile kernel.
+//   MODE_BASE : tile t covers [t*L, t*L+L) with L <= CAP.  Keys are sorted in
+//               registers (ITEMS per thread), then merged in shared memory up
+//               to the whole tile.  A short last tile is padded with copies of
+//               its own largest key, which sort after every real key, so no
+//               sentinel value is reserved.
+//   MODE_GROUP: CTA g merges the K runs of group g (K*L <= CAP).
+//   MODE_TILE : CTA merges one tile of a group whose runs are cut by `desc`.
+// STABLE: equivalent keys keep their input order (used for key/value sorts and
+// for user comparators whose equivalent keys may differ in their bits).
+template <class K, class V, class Cmp, class Codec, int MODE, bool STABLE, int NT, int ITEMS>
+__global__ void __launch_bounds__(NT) tile_kernel(TileArgs<K, V> a) {
+  constexpr int CAP = NT * ITEMS;
+  constexpr bool kHasVal = HasVal<V>::value;
+  using L = TileSmemLayout<K, V, CAP>;
+  extern __shared__ __align__(16) unsigned char smem[];
+  K* sk = reinterpret_cast<K*>(smem);
+  V* sv = reinterpret_cast<V*>(smem + L::key_bytes);
+  int* pre = reinterpret_cast<int*>(smem + L::key_bytes + L::val_bytes);
+  int64_t* gs = reinterpret_cast<int64_t*>(smem + L::key_bytes + L::val_bytes + L::pre_bytes);
+  const Cmp cmp;
+  const int tid = threadIdx.x;
+
+  int64_t out_base;   // global index of this tile's first output
+  int64_t run_base;   // global index of the output run this tile belongs to
+  int64_t run_index;  // index of that output run
+  int cnt;            // keys in this tile
+  int nk = 1;         // runs in the tile (GROUP/TILE)
+
+  K ok[ITEMS];
+  V ov[ITEMS];
+
+  if constexpr (MODE == MODE_BASE) {
+    const int64_t base = (int64_t)blockIdx.x * a.L;
+    if (base >= a.n) return;
+    cnt = (int)min64(a.L, a.n - base);
+    out_base = base;
+    run_base = base;
+    run_index = blockIdx.x;
+    // Coalesced striped load: register i of thread t holds element t + i*NT.
+    K r[ITEMS];
+    V rv[ITEMS];
+    if constexpr (STABLE) {
+      // Stable: each thread must own a contiguous chunk of the input, so the
+      // striped load is staged through shared memory.
+#pragma unroll
+      for (int i = 0; i < ITEMS; ++i) {
+        const int p = tid + i * NT;
+        if (p < cnt) {
+          sk[p] = maybe_enc<Codec>(a.in[base + p], a.enc_on_load);
+          if constexpr (kHasVal) sv[p] = a.gen_index ? (V)(base + p) : a.vin[base + p];
+        }
+      }
+      __syncthreads();
+#pragma unroll
+      for (int i = 0; i < ITEMS; ++i) {
+        const int p = tid * ITEMS + i;
+        r[i] = sk[p < cnt ? p : 0];
+        if constexpr (kHasVal) rv[i] = sv[p < cnt ? p : 0];
+      }
+      if (cnt < CAP) {
+        K m = r[0];
+#pragma unroll
+        for (int i = 1; i < ITEMS; ++i) {
+          if (tid * ITEMS + i < cnt) m = cmp(m, r[i]) ? r[i] : m;
+        }
+        __syncthreads();  // every chunk is in registers; sk is free as scratch
+        m = block_max<NT>(m, sk, cmp);
+#pragma unroll
+        for (int i = 0; i < ITEMS; ++i) {
+          if (tid * ITEMS + i >= cnt) r[i] = m;
+        }
+      }
+      transposition_sort<ITEMS>(r, rv, cmp);
+      __syncthreads();
+    } else {
+#pragma unroll
+      for (int i = 0; i < ITEMS; ++i) {
+        const int p = tid + i * NT;
+        if (p < cnt) r[i] = maybe_enc<Codec>(a.in[base + p], a.enc_on_load);
+      }
+      if (cnt < CAP) {
+        K m = r[0];
+        if (tid >= cnt) m = maybe_enc<Codec>(a.in[base], a.enc_on_load);
+#pragma unroll
+        for (int i = 1; i < ITEMS; ++i) {
+          if (tid + i * NT < cnt) m = cmp(m, r[i]) ? r[i] : m;
+        }
+        m = block_max<NT>(m, sk, cmp);
+#pragma unroll
+        for (int i = 0; i < ITEMS; ++i) {
+          if (tid + i * NT >= cnt) r[i] = m;
+        }
+      }
+      network_sort<ITEMS>(r, cmp);
+    }
+    // Blocked write: thread t's sorted run at [t*ITEMS, t*ITEMS+ITEMS).
+    // ITEMS is odd, so the ITEMS-strided stores hit distinct banks.
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i) {
+      sk[tid * ITEMS + i] = r[i];
+      if constexpr (kHasVal) sv[tid * ITEMS + i] = rv[i];
+    }
+    __syncthreads();
+    // Merge levels up to the whole (padded) tile.
+    const int s = tid * ITEMS;
+    for (int rl = ITEMS; rl < CAP; rl *= 2) {
+      merge_level_regular<ITEMS>(sk, sv, CAP, rl, s, ok, ov, cmp);
+      __syncthreads();
+#pragma unroll
+      for (int i = 0; i < ITEMS; ++i) {
+        sk[s + i] = ok[i];
+        if constexpr (kHasVal) sv[s + i] = ov[i];
+      }
+      __syncthreads();
+    }
+  } else {
+    // ---- GROUP / TILE: gather the K input segments into shared memory ----
+    int64_t gbase;
+    int64_t tile_off = 0;  // group-relative output offset
+    int64_t g;
+    if constexpr (MODE == MODE_GROUP) {
+      g = blockIdx.x;
+      gbase = g * a.L * a.k;
+      if (gbase >= a.n) return;
+      const int64_t ng = min64(a.L * a.k, a.n - gbase);
+      cnt = (int)ng;
+      nk = a.k;
+      if (tid <= nk) pre[tid] = (int)min64((int64_t)tid * a.L, ng);
+      const K* src = a.in + gbase;
+      for (int p = tid; p < cnt; p += NT) {
+        sk[p] = maybe_enc<Codec>(src[p], a.enc_on_load);
+        if constexpr (kHasVal) sv[p] = a.gen_index ? (V)(gbase + p) : a.vin[gbase + p];
+      }
+    } else {
+      const int64_t tau = blockIdx.x;
+      g = tau / a.tiles_full;
+      const int64_t j = tau - g * a.tiles_full;
+      const int64_t jg = (g == a.groups - 1) ? a.tiles_last : a.tiles_full;
+      if (j >= jg) return;
+      gbase = g * a.L * a.k;
+      const int64_t row = g * (a.tiles_full + 1) + j;
+      nk = a.k;
+      const int64_t ng = min64(a.L * a.k, a.n - gbase);
+      if (tid < 32) {
+        int len = 0;
+        if (tid < nk) {
+          const int64_t lo = a.desc[row * nk + tid];
+          const int64_t hi = a.desc[(row + 1) * nk + tid];
+          // a segment must lie inside its run and hold at most CAP keys
+          const int64_t rl = min64(a.L, ng - min64((int64_t)tid * a.L, ng));
+          const bool ok_seg = (lo >= 0) && (hi >= lo) && (hi <= rl) && (hi - lo <= CAP);
+          len = ok_seg ? (int)(hi - lo) : 0;
+          if (!ok_seg) {
+            len = CAP + 1;  // forces the capacity check below to reject the tile
+            if (a.err) atomicOr(a.err, DEV_BAD_SEGMENT);
+          }
+          gs[tid] = gbase + (int64_t)tid * a.L + lo;
+        }
+        // inclusive scan of segment lengths across the warp
+        int incl = len;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(0xffffffffu, incl, o);
+          if (tid >= o) incl += y;
+        }
+        if (tid < nk) pre[tid + 1] = incl;
+        if (tid == 0) pre[0] = 0;
+      }
+      tile_off = a.doff[row];
+      __syncthreads();
+      cnt = pre[nk];
+      if (cnt > CAP || cnt < 0) {
+        // never overrun the shared-memory tile: report and skip
+        if (tid == 0 && a.err) atomicOr(a.err, DEV_TILE_OVERFLOW);
+        return;
+      }
+      for (int kk = 0; kk < nk; ++kk) {
+        const int b = pre[kk];
+        const int len = pre[kk + 1] - b;
+        const int64_t src = gs[kk];
+        for (int i = tid; i < len; i += NT) {
+          sk[b + i] = maybe_enc<Codec>(a.in[src + i], a.enc_on_load);
+          if constexpr (kHasVal) sv[b + i] = a.gen_index ? (V)(src + i) : a.vin[src + i];
+        }
+      }
+    }
+    out_base = gbase + tile_off;
+    run_base = gbase;
+    run_index = g;
+    __syncthreads();
+    // ---- ceil(log2 nk) levels of pairwise merging ----
+    const int s = tid * ITEMS;
+    const int e = min(s + ITEMS, cnt);
+    for (int span = 2; span < 2 * nk; span *= 2) {
+      if (s < cnt) merge_level_var<ITEMS>(sk, sv, pre, nk, span, s, e, ok, ov, cmp);
+      __syncthreads();
+      if (s < cnt) {
+#pragma unroll
+        for (int i = 0; i < ITEMS; ++i) {
+          if (s + i < e) {
+            sk[s + i] = ok[i];
+            if constexpr (kHasVal) sv[s + i] = ov[i];
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+
+  // ---- coalesced store of the merged tile (+ block sample) ----
+  for (int p = tid; p < cnt; p += NT) {
+    a.out[out_base + p] = maybe_dec<Codec>(sk[p], a.dec_on_store);
+    if constexpr (kHasVal) a.vout[out_base + p] = sv[p];
+  }
+  if (a.sample_out) {
+    // output positions whose offset in the output run is a multiple of B
+    const int64_t rel0 = out_base - run_base;
+    const int64_t first = (a.sample_b - rel0 % a.sample_b) % a.sample_b;
+    for (int64_t p = first + (int64_t)tid * a.sample_b; p < cnt; p += (int64_t)NT * a.sample_b) {
+      a.sample_out[run_index * a.sample_run_len + (rel0 + p) / a.sample_b] = sk[p];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Splitter: exact tile boundaries of one merge round.
+//
+// For group g the merged block sample F (the first key of every B-key block of
+// every run, merged in (key, run, block) order) is cut every G entries.  The
+// first key of block F[j*G] is boundary j.  One warp per boundary; lane k finds
+// how many keys of run k precede the boundary in the stable (key, run, index)
+// order by binary search over run k.  Between two boundaries every run
+// contributes at most (its blocks in that stretch of F + 1) blocks, so a tile
+// holds at most (G + K) * B keys.
+template <class K, class Cmp, class Codec>
+__global__ void __launch_bounds__(256) splitter_kernel(const K* __restrict__ data, const K* __restrict__ fkeys,
+                                                        const uint32_t* __restrict__ fidx, int64_t n, int64_t L,
+                                                        int k, int64_t sample_run_len, int sample_b, int64_t G,
+                                                        int64_t tiles_full, int64_t tiles_last, int64_t groups,
+                                                        int64_t* __restrict__ desc, int64_t* __restrict__ doff,
+                                                        int enc) {
+  const Cmp cmp;
+  const int lane = threadIdx.x & 31;
+  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t rows_per_group = tiles_full + 1;
+  const int64_t g = row / rows_per_group;
+  if (g >= groups) return;
+  const int64_t j = row - g * rows_per_group;
+  const int64_t jg = (g == groups - 1) ? tiles_last : tiles_full;
+  if (j > jg) return;
+  const int64_t gbase = g * L * k;
+  const int64_t ng = min64(L * k, n - gbase);
+  int64_t c = 0;
+  if (lane < k) {
+    const int64_t rs = min64((int64_t)lane * L, ng);
+    const int64_t re = min64((int64_t)(lane + 1) * L, ng);
+    const int64_t len = re - rs;
+    if (j == 0) {
+      c = 0;
+    } else if (j == jg) {
+      c = len;
+    } else {
+      const int64_t fpos = g * (int64_t)k * sample_run_len + j * G;
+      const K v = fkeys[fpos];
+      const int64_t sidx = (int64_t)fidx[fpos];
+      const int64_t run = sidx / sample_run_len;
+      const int64_t kb = run - g * k;
+      const int64_t ib = (sidx - run * sample_run_len) * sample_b;
+      if (lane == kb) {
+        c = ib;
+      } else {
+        const K* r = data + gbase + rs;
+        int64_t lo = 0, hi = len;
+        if (lane < kb) {
+          // keys <= v come first (earlier run wins ties)
+          while (lo < hi) {
+            const int64_t mid = (lo + hi) >> 1;
+            if (!cmp(v, maybe_enc<Codec>(r[mid], enc))) lo = mid + 1; else hi = mid;
+          }
+        } else {
+          // keys < v come first
+          while (lo < hi) {
+            const int64_t mid = (lo + hi) >> 1;
+            if (cmp(maybe_enc<Codec>(r[mid], enc), v)) lo = mid + 1; else hi = mid;
+          }
+        }
+        c = lo;
+      }
+    }
+    desc[row * k + lane] = c;
+  }
+  // group-relative output offset of the tile that starts at this boundary
+  int64_t sum = c;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  if (lane == 0) doff[row] = sum;
+}
+
+// ---------------------------------------------------------------------------
+// Block sample of a sample: out[r*out_run + b] = in[r*in_run + b*B] for every
+// run r and every b < ceil(len_r / B).
+template <class K, class Codec>
+__global__ void gather_sample_kernel(const K* __restrict__ in, K* __restrict__ out, int64_t n_in, int64_t in_run,
+                                     int64_t out_run, int b_step, int64_t n_out_slots, int enc) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_out_slots) return;
+  const int64_t r = t / out_run;
+  const int64_t b = t - r * out_run;
+  const int64_t src = r * in_run + b * b_step;
+  const int64_t rend = min64((r + 1) * in_run, n_in);
+  if (src < rend) out[t] = maybe_enc<Codec>(in[src], enc);
+}
+
+// Exact co-ranks at arbitrary output ranks of one K-way task, given the task
+// merged with its origin index.  Lane k counts the keys of run k that precede
+// or equal the rank-th smallest element (stable order).  Mirrors the contract
+// of findPartitions (warp-partition.hxx:488-532) for caller-chosen ranks.
+template <class K, class Cmp, class Codec>
+__global__ void corank_kernel(const K* __restrict__ task, const K* __restrict__ merged,
+                              const uint32_t* __restrict__ origin, int64_t size, int k, int64_t task_size,
+                              const int64_t* __restrict__ ranks, int64_t nranks, int64_t* __restrict__ out) {
+  const Cmp cmp;
+  const int lane = threadIdx.x & 31;
+  const int64_t q = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (q >= nranks) return;
+  int64_t r = ranks[q];
+  r = r < 0 ? 0 : (r > task_size ? task_size : r);
+  for (int kk = lane; kk < k; kk += 32) {
+    const int64_t rs = min64((int64_t)kk * size, task_size);
+    const int64_t re = min64((int64_t)(kk + 1) * size, task_size);
+    int64_t c = 0;
+    if (r > 0) {
+      const K v = merged[r - 1];
+      const int64_t o = (int64_t)origin[r - 1];
+      const int64_t kb = o / size;
+      if (kk == kb) {
+        c = o - kb * size + 1;
+      } else {
+        const K* run = task + rs;
+        int64_t lo = 0, hi = re - rs;
+        if (kk < kb) {
+          while (lo < hi) {
+            const int64_t mid = (lo + hi) >> 1;
+            if (!cmp(v, Codec::enc(run[mid]))) lo = mid + 1; else hi = mid;
+          }
+        } else {
+          while (lo < hi) {
+            const int64_t mid = (lo + hi) >> 1;
+            if (cmp(Codec::enc(run[mid]), v)) lo = mid + 1; else hi = mid;
+          }
+        }
+        c = lo;
+      }
+    }
+    out[q * k + kk] = c;
+  }
+}
+
+}  // namespace gms

@@ -1,0 +1,267 @@
+"""Python binding of the GB300 multiway mergesort C ABI (include/gms.h).
+
+Builds libgms.so from csrc/ with nvcc for sm_103a and exposes the C entry
+points through ctypes.  PyTorch supplies device memory and the current CUDA
+stream; no compute happens in Python.  There is no CPU fallback: if the shared
+library is missing or fails to load, every call raises.
+
+Reference interface mirrored: multimergesort<T,cmp>(input, output, host_array,
+threadBlocks, N) (GPU-MMS src/multimergesort.hxx:56-141, README.md:16-25),
+squareSort (src/basecase/squareSort.hxx:62-131), one merge round
+(src/multimergesort.hxx:87-135, 155-209) and findPartitions
+(src/warp-partition.hxx:488-532).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import threading
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "libgms.so")
+INCLUDE = os.path.join(ROOT, "include")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC"]
+UNITS = ["gms_capi_misc.cu", "gms_capi_k32.cu", "gms_capi_k64.cu", "gms_capi_kv.cu"]
+
+GMS_OK = 0
+DTYPES = {"int32": 0, "uint32": 1, "float32": 2, "int64": 3, "uint64": 4, "float64": 5}
+
+
+class GmsError(RuntimeError):
+    """A C-ABI call returned a non-zero gms_status."""
+
+    def __init__(self, status, where, message):
+        super().__init__(f"{where}: status {status}: {message}")
+        self.status = status
+
+
+def _nvcc():
+    for cand in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", "nvcc"):
+        if cand and (os.path.sep not in cand or os.path.exists(cand)):
+            return cand
+    return "nvcc"
+
+
+def _sources():
+    out = []
+    for d in (CSRC, INCLUDE):
+        for f in os.listdir(d):
+            if f.endswith((".cu", ".cuh", ".h", ".hxx")):
+                out.append(os.path.join(d, f))
+    return out
+
+
+def build(force=False, jobs=None, verbose=False):
+    """Compile csrc/*.cu for sm_103a into libgms.so (in-tree)."""
+    os.makedirs(BUILD, exist_ok=True)
+    newest = max(os.path.getmtime(p) for p in _sources())
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= newest:
+        return LIB
+    nvcc = _nvcc()
+
+    def compile_one(unit):
+        obj = os.path.join(BUILD, unit.replace(".cu", ".o"))
+        cmd = [nvcc] + NVCC_FLAGS + ["-c", os.path.join(CSRC, unit), "-o", obj]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed for {unit}:\n{r.stdout}\n{r.stderr}")
+        if verbose:
+            print(r.stdout, r.stderr)
+        return obj
+
+    with ThreadPoolExecutor(max_workers=jobs or len(UNITS)) as ex:
+        objs = list(ex.map(compile_one, UNITS))
+    tmp = LIB + ".tmp"
+    cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+# ---------------------------------------------------------------------------
+# ctypes declarations: name -> (restype, argtypes)
+_i32, _i64, _u64, _vp, _sz = ctypes.c_int, ctypes.c_int64, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_size_t
+SIGNATURES = {
+    "gms_version": (_i32, []),
+    "gms_status_string": (ctypes.c_char_p, [_i32]),
+    "gms_last_error": (ctypes.c_char_p, []),
+    "gms_sort_i32": (_i32, [_vp, _vp, _i64, _i32, _vp]),
+    "gms_sort_u32": (_i32, [_vp, _vp, _i64, _i32, _vp]),
+    "gms_sort_i64": (_i32, [_vp, _vp, _i64, _i32, _vp]),
+    "gms_sort_u64": (_i32, [_vp, _vp, _i64, _i32, _vp]),
+    "gms_sort_f32": (_i32, [_vp, _vp, _i64, _i32, _vp]),
+    "gms_sort_f64": (_i32, [_vp, _vp, _i64, _i32, _vp]),
+    "gms_sort_kv_i32_i32": (_i32, [_vp, _vp, _vp, _vp, _i64, _i32, _vp]),
+    "gms_sort_kv_u32_i32": (_i32, [_vp, _vp, _vp, _vp, _i64, _i32, _vp]),
+    "gms_sort_kv_f32_i32": (_i32, [_vp, _vp, _vp, _vp, _i64, _i32, _vp]),
+    "gms_sort_kv_i64_i32": (_i32, [_vp, _vp, _vp, _vp, _i64, _i32, _vp]),
+    "gms_sort_kv_u64_i32": (_i32, [_vp, _vp, _vp, _vp, _i64, _i32, _vp]),
+    "gms_sort_kv_f64_i32": (_i32, [_vp, _vp, _vp, _vp, _i64, _i32, _vp]),
+    "gms_sort_host_i32": (_i32, [_vp, _vp, _i64, _vp]),
+    "gms_sort_host_kv_u64_i32": (_i32, [_vp, _vp, _vp, _vp, _i64, _vp]),
+    "gms_tile_sort_i32": (_i32, [_vp, _i64, _i64, _vp]),
+    "gms_tile_sort_u64": (_i32, [_vp, _i64, _i64, _vp]),
+    "gms_max_tile": (_i64, []),
+    "gms_merge_level_i32": (_i32, [_vp, _vp, _i64, _i64, _i32, _vp]),
+    "gms_merge_level_u64": (_i32, [_vp, _vp, _i64, _i64, _i32, _vp]),
+    "gms_find_partitions_i32": (_i32, [_vp, _i64, _i32, _i64, _vp, _i64, _vp, _vp]),
+    "gms_workspace_bytes": (_sz, [_i32, _i32, _i64]),
+    "gms_reserve": (_i32, [_i32, _i32, _i64, _vp]),
+    "gms_device_status": (_i32, [_vp, ctypes.POINTER(ctypes.c_int)]),
+    "gms_release_workspaces": (None, []),
+    "gms_rounds": (_i32, [_i32, _i32, _i64]),
+    "gms_base_tile": (_i64, [_i32, _i32]),
+}
+
+_lock = threading.Lock()
+_lib = None
+
+
+def load(path=None):
+    """Load libgms.so (raises if it is missing: there is no fallback)."""
+    global _lib
+    with _lock:
+        if _lib is not None and path is None:
+            return _lib
+        p = path or LIB
+        if not os.path.exists(p):
+            raise OSError(f"{p} not found: build it with gms.build() (nvcc, sm_103a)")
+        lib = ctypes.CDLL(p)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        if path is None:
+            _lib = lib
+        return lib
+
+
+def _check(status, where):
+    if status != GMS_OK:
+        lib = load()
+        raise GmsError(status, where, lib.gms_last_error().decode(errors="replace"))
+
+
+# ---------------------------------------------------------------------------
+# torch-facing helpers (device tensors, current stream)
+def _stream_ptr(stream=None):
+    import torch
+
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+_SUFFIX = {"torch.int32": "i32", "torch.uint32": "u32", "torch.float32": "f32", "torch.int64": "i64",
+           "torch.uint64": "u64", "torch.float64": "f64"}
+
+
+def _suffix(t):
+    s = _SUFFIX.get(str(t.dtype))
+    if s is None:
+        raise TypeError(f"unsupported key dtype {t.dtype}")
+    return s
+
+
+def _dev_check(*ts):
+    for t in ts:
+        if not t.is_cuda or not t.is_contiguous():
+            raise ValueError("tensors must be contiguous CUDA tensors")
+
+
+def sort_(inp, out, thread_blocks=0, stream=None):
+    """multimergesort: sorts `inp` into `out` (both device, same dtype/size).
+    `inp` is clobbered.  Returns `out`."""
+    _dev_check(inp, out)
+    if inp.numel() != out.numel() or inp.dtype != out.dtype:
+        raise ValueError("input/output mismatch")
+    lib = load()
+    fn = getattr(lib, "gms_sort_" + _suffix(inp))
+    _check(fn(inp.data_ptr(), out.data_ptr(), inp.numel(), thread_blocks, _stream_ptr(stream)), fn.__name__)
+    return out
+
+
+def sort(t, stream=None):
+    """Returns a sorted copy of device tensor `t` (t is left intact)."""
+    import torch
+
+    inp = t.clone()
+    out = torch.empty_like(t)
+    return sort_(inp, out, stream=stream)
+
+
+def sort_kv_(kin, vin, kout, vout, thread_blocks=0, stream=None):
+    """Stable key/value sort (int32 payload); inputs clobbered."""
+    _dev_check(kin, vin, kout, vout)
+    if str(vin.dtype) != "torch.int32":
+        raise TypeError("payload must be int32")
+    lib = load()
+    fn = getattr(lib, "gms_sort_kv_" + _suffix(kin) + "_i32")
+    _check(fn(kin.data_ptr(), vin.data_ptr(), kout.data_ptr(), vout.data_ptr(), kin.numel(), thread_blocks,
+              _stream_ptr(stream)), fn.__name__)
+    return kout, vout
+
+
+def sort_kv(keys, vals, stream=None):
+    import torch
+
+    ki, vi = keys.clone(), vals.clone()
+    ko, vo = torch.empty_like(keys), torch.empty_like(vals)
+    return sort_kv_(ki, vi, ko, vo, stream=stream)
+
+
+def tile_sort_(data, tile, stream=None):
+    """squareSort contract: every `tile`-key tile sorted in place."""
+    _dev_check(data)
+    lib = load()
+    fn = {"i32": lib.gms_tile_sort_i32, "u64": lib.gms_tile_sort_u64}[_suffix(data)]
+    _check(fn(data.data_ptr(), data.numel(), tile, _stream_ptr(stream)), "tile_sort")
+    return data
+
+
+def merge_level(inp, run_len, k, stream=None):
+    """One K-way merge round over runs of `run_len`; returns a new tensor."""
+    import torch
+
+    _dev_check(inp)
+    out = torch.empty_like(inp)
+    lib = load()
+    fn = {"i32": lib.gms_merge_level_i32, "u64": lib.gms_merge_level_u64}[_suffix(inp)]
+    _check(fn(inp.data_ptr(), out.data_ptr(), inp.numel(), run_len, k, _stream_ptr(stream)), "merge_level")
+    return out
+
+
+def find_partitions(task, size, k, ranks, stream=None):
+    """findPartitions contract: per rank, the keys each of the k runs gives."""
+    import torch
+
+    _dev_check(task, ranks)
+    out = torch.empty((ranks.numel(), k), dtype=torch.int64, device=task.device)
+    lib = load()
+    _check(lib.gms_find_partitions_i32(task.data_ptr(), size, k, task.numel(), ranks.data_ptr(), ranks.numel(),
+                                       out.data_ptr(), _stream_ptr(stream)), "find_partitions")
+    return out
+
+
+def device_status(stream=None):
+    """Waits for the stream and returns (and clears) the device status word."""
+    lib = load()
+    v = ctypes.c_int(0)
+    _check(lib.gms_device_status(_stream_ptr(stream), ctypes.byref(v)), "device_status")
+    return v.value
+
+
+def sort_host_i32(host_in, host_out, stream=None):
+    """End-to-end: host int32 array in, sorted host array out (waits)."""
+    lib = load()
+    _check(lib.gms_sort_host_i32(host_in.data_ptr(), host_out.data_ptr(), host_in.numel(), _stream_ptr(stream)),
+           "sort_host_i32")
+    return host_out

@@ -1,0 +1,168 @@
+/*
+ * gms.h -- C ABI of the GB300 multiway mergesort (libgms.so).
+ *
+ * Plain pointers and sizes only.  Every device pointer is a CUDA global-memory
+ * pointer on the current device; `stream` is a cudaStream_t passed as void*
+ * (NULL = legacy default stream).  Every call returns a gms_status (0 = OK) and
+ * records a message readable with gms_last_error() on the calling thread.
+ * Calls are asynchronous on `stream` unless stated otherwise.
+ *
+ * Each entry point names the GPU-MMS interface it replaces (paths relative to
+ * the GPU-MMS source tree).
+ */
+#ifndef GMS_H_
+#define GMS_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum gms_status {
+  GMS_OK = 0,
+  GMS_ERR_INVALID = 1,   /* bad argument: null pointer, negative size, bad fan-in ... */
+  GMS_ERR_CUDA = 2,      /* a CUDA call failed; gms_last_error() has the CUDA message */
+  GMS_ERR_NOMEM = 3,     /* device scratch could not be allocated                      */
+  GMS_ERR_TOO_LARGE = 4, /* size beyond what this build supports                       */
+  GMS_ERR_INTERNAL = 5
+} gms_status;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int gms_version(void);
+/* Human-readable name of a status code. */
+const char* gms_status_string(int status);
+/* Last error message recorded on the calling thread ("" if none). */
+const char* gms_last_error(void);
+
+/* ---------------------------------------------------------------------------
+ * Plain sorts.
+ *
+ * Replaces: template<typename T, fptr_t f> T* multimergesort(T* input,
+ *   T* output, T* h_data, int N)            src/multimergesort.hxx:56-141
+ * and the documented 5-argument form multimergesort<T,cmp>(input, output,
+ *   host_array, threadBlocks, N)             README.md:16-25
+ *
+ * Sorts `n` keys ascending.  `input` and `output` are device arrays of n keys.
+ * The sorted keys are ALWAYS in `output` (the reference returns whichever of
+ * its two buffers holds the result; here that buffer is always `output`).
+ * `input` is used as scratch and its contents are clobbered, as in the
+ * reference.  `thread_blocks` is the reference's threadBlocks hint: <= 0 lets
+ * the library choose; a positive value is accepted and recorded (the grids of
+ * this implementation are sized by the data).  Signed integers sort by value;
+ * f32/f64 sort by IEEE-754 totalOrder (-NaN < -Inf < ... < -0 < +0 < ... <
+ * +Inf < +NaN).  The full key range is valid (no reserved sentinel such as the
+ * reference's MAXVAL, src/cmp.hxx:26).
+ * ------------------------------------------------------------------------- */
+int gms_sort_i32(int32_t* input, int32_t* output, int64_t n, int thread_blocks, void* stream);
+int gms_sort_u32(uint32_t* input, uint32_t* output, int64_t n, int thread_blocks, void* stream);
+int gms_sort_i64(int64_t* input, int64_t* output, int64_t n, int thread_blocks, void* stream);
+int gms_sort_u64(uint64_t* input, uint64_t* output, int64_t n, int thread_blocks, void* stream);
+int gms_sort_f32(float* input, float* output, int64_t n, int thread_blocks, void* stream);
+int gms_sort_f64(double* input, double* output, int64_t n, int thread_blocks, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Key/value sorts: keys with an int32 payload, stable (equal keys keep their
+ * input order), i.e. the order of std::stable_sort by key.
+ *
+ * Replaces: the packed key/value DATATYPE of the plugin surface (a 32-bit key
+ * and 32-bit value cast to 64 bits for __shfl), src/cmp.hxx:59-73, sorted by
+ * multimergesort, src/multimergesort.hxx:56-141.
+ *
+ * keys_in/vals_in are clobbered; the result is in keys_out/vals_out.
+ * ------------------------------------------------------------------------- */
+int gms_sort_kv_i32_i32(int32_t* keys_in, int32_t* vals_in, int32_t* keys_out, int32_t* vals_out, int64_t n,
+                        int thread_blocks, void* stream);
+int gms_sort_kv_u32_i32(uint32_t* keys_in, int32_t* vals_in, uint32_t* keys_out, int32_t* vals_out, int64_t n,
+                        int thread_blocks, void* stream);
+int gms_sort_kv_f32_i32(float* keys_in, int32_t* vals_in, float* keys_out, int32_t* vals_out, int64_t n,
+                        int thread_blocks, void* stream);
+int gms_sort_kv_i64_i32(int64_t* keys_in, int32_t* vals_in, int64_t* keys_out, int32_t* vals_out, int64_t n,
+                        int thread_blocks, void* stream);
+int gms_sort_kv_u64_i32(uint64_t* keys_in, int32_t* vals_in, uint64_t* keys_out, int32_t* vals_out, int64_t n,
+                        int thread_blocks, void* stream);
+int gms_sort_kv_f64_i32(double* keys_in, int32_t* vals_in, double* keys_out, int32_t* vals_out, int64_t n,
+                        int thread_blocks, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * End-to-end sorts from host memory: copy n keys from `host_in` to the device,
+ * sort, copy the result to `host_out` (may equal host_in), and wait for the
+ * stream.  Device buffers come from the library's per-stream cache (allocated
+ * on first use, reused afterwards).  Pinned host memory gives full copy speed.
+ *
+ * Replaces: the reference's driver sequence cudaMemcpy H2D -> multimergesort
+ * -> cudaMemcpy D2H, src/testMM.cu:167-195.
+ * ------------------------------------------------------------------------- */
+int gms_sort_host_i32(const int32_t* host_in, int32_t* host_out, int64_t n, void* stream);
+int gms_sort_host_kv_u64_i32(const uint64_t* keys_in, const int32_t* vals_in, uint64_t* keys_out,
+                             int32_t* vals_out, int64_t n, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Base case alone: every `tile`-key tile of `data` sorted in place, plus the
+ * short tail tile (1 <= tile <= gms_max_tile()).
+ *
+ * Replaces: squareSort<T,f><<<N/M, ...>>>(data, N)
+ *   src/basecase/squareSort.hxx:62-131 (tile M = 1024, tail 69-87).
+ * ------------------------------------------------------------------------- */
+int gms_tile_sort_i32(int32_t* data, int64_t n, int64_t tile, void* stream);
+int gms_tile_sort_u64(uint64_t* data, int64_t n, int64_t tile, void* stream);
+/* Largest tile the base case sorts in one CTA (keys of 4 bytes). */
+int64_t gms_max_tile(void);
+
+/* ---------------------------------------------------------------------------
+ * One merge round: every group of `k` consecutive sorted runs of `run_len`
+ * keys (the last run and the last group may be short) merged into one sorted
+ * run of up to k*run_len keys, stably (earlier run first on ties).
+ * 2 <= k <= 32.  `input` is not modified.
+ *
+ * Replaces: one iteration of the round loop, src/multimergesort.hxx:87-135:
+ *   findPartitions + multimergeLevel<T,f>(data, output, pivots, size, tasks)
+ *   src/multimergesort.hxx:155-209, src/io-merge-gen.hxx:306-355.
+ * ------------------------------------------------------------------------- */
+int gms_merge_level_i32(const int32_t* input, int32_t* output, int64_t n, int64_t run_len, int k, void* stream);
+int gms_merge_level_u64(const uint64_t* input, uint64_t* output, int64_t n, int64_t run_len, int k, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Splitter: for one task of `k` sorted runs of `size` keys (`task_size` keys in
+ * all; the last run may be short) and each target output rank r in `ranks`
+ * (device, `nranks` entries), the number of keys each run contributes to the
+ * first r outputs of the stable merge: out[q*k + j] (device, int64).
+ * Ranks are clamped to [0, task_size].
+ *
+ * Replaces: findPartitions<T,f>(data, pivots, size, tasks, edgeCaseTaskSize)
+ *   src/warp-partition.hxx:488-532 (single_pivot_partition 179-366), whose
+ *   targets are the equal shares mergerIdInTask*taskSize/mergersPerTask
+ *   (warp-partition.hxx:234); callers pass those ranks explicitly.
+ * ------------------------------------------------------------------------- */
+int gms_find_partitions_i32(const int32_t* task, int64_t size, int k, int64_t task_size, const int64_t* ranks,
+                            int64_t nranks, int64_t* out, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Scratch management.  Sorts draw device scratch from a per-(device, stream)
+ * cache that grows on demand; reserve it ahead of CUDA-graph capture with
+ * gms_reserve().  gms_release_workspaces() frees every cached buffer (call it
+ * only when no sort is in flight).
+ * ------------------------------------------------------------------------- */
+/* dtype codes: 0=i32 1=u32 2=f32 3=i64 4=u64 5=f64; kv: 1 = with int32 payload */
+size_t gms_workspace_bytes(int dtype, int kv, int64_t n);
+int gms_reserve(int dtype, int kv, int64_t n, void* stream);
+void gms_release_workspaces(void);
+
+/* Waits for `stream`, then reads and clears the device status word of the
+ * stream's scratch: 0 = no kernel reported a problem; bit 0 = a tile exceeded
+ * the shared-memory capacity and was skipped; bit 1 = a tile boundary lay
+ * outside its run.  Either bit means the result is wrong (never expected).
+ * No reference counterpart (the reference reports nothing from its kernels). */
+int gms_device_status(void* stream, int* status_out);
+
+/* Number of merge rounds (after the base case) a sort of n keys of the given
+ * dtype performs, and the base tile (keys) it uses. */
+int gms_rounds(int dtype, int kv, int64_t n);
+int64_t gms_base_tile(int dtype, int kv);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GMS_H_ */

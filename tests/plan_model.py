@@ -1,0 +1,134 @@
+"""CPU model of the round/tile index arithmetic of the CUDA library.
+
+Not the oracle: this restates the library's OWN plan (gpu-mms_gb300/csrc/
+gms_sort.cuh: Engine::round / Engine::sort) and the index math of
+splitter_kernel and tile_kernel (gms_kernels.cuh) in numpy, so that the
+bounds every launch relies on -- above all "a tile never holds more than CAP
+keys", which sizes the shared-memory buffer -- can be checked on the CPU for
+any geometry (CAP, K, B) and any input distribution before code runs on a GPU.
+"""
+import numpy as np
+
+
+def ceil_div(a, b):
+    return -(-a // b)
+
+
+class Geometry:
+    def __init__(self, cap, k, b):
+        self.cap, self.k, self.b = cap, k, b
+        self.g = cap // b - k
+        assert self.g > 0, "tile geometry needs CAP/B > K"
+
+
+def _stable_merge(keys, idx):
+    order = np.argsort(keys, kind="stable")
+    return keys[order], idx[order]
+
+
+def model_round(keys, idx, L, geo, stats, level=0):
+    """One K-way round over runs of length L.  Returns merged (keys, idx).
+
+    Mirrors Engine::round: GROUP mode when K*L <= CAP, else sample -> recursive
+    merge of the sample with its positions -> boundaries -> tiles.
+    """
+    n = len(keys)
+    k, B, cap, G = geo.k, geo.b, geo.cap, geo.g
+    out_k = np.empty_like(keys)
+    out_i = np.empty_like(idx)
+    if k * L <= cap:
+        for gb in range(0, n, k * L):
+            ge = min(n, gb + k * L)
+            assert ge - gb <= cap
+            out_k[gb:ge], out_i[gb:ge] = _stable_merge(keys[gb:ge], idx[gb:ge])
+        stats["group_launches"] = stats.get("group_launches", 0) + 1
+        return out_k, out_i
+    runs = ceil_div(n, L)
+    Ls = ceil_div(L, B)
+    ns = (runs - 1) * Ls + ceil_div(n - (runs - 1) * L, B)
+    # block sample: run r, block b -> slot r*Ls + b (gather_sample_kernel)
+    S = np.empty(ns, dtype=keys.dtype)
+    for r in range(runs):
+        rs, re = r * L, min(n, (r + 1) * L)
+        samp = keys[rs:re:B]
+        S[r * Ls:r * Ls + len(samp)] = samp
+        if r < runs - 1:
+            assert len(samp) == Ls
+    fk, fi = model_round(S, np.arange(ns, dtype=np.int64), Ls, geo, stats, level + 1)
+    groups = ceil_div(n, L * k)
+    tiles_full = ceil_div(k * Ls, G)
+    last_ns = ns - (groups - 1) * k * Ls
+    tiles_last = ceil_div(last_ns, G)
+    max_tile = 0
+    for g in range(groups):
+        gbase = g * L * k
+        ng = min(L * k, n - gbase)
+        jg = tiles_last if g == groups - 1 else tiles_full
+        desc = np.zeros((jg + 1, k), dtype=np.int64)
+        lens = [max(0, min((kk + 1) * L, ng) - min(kk * L, ng)) for kk in range(k)]
+        for j in range(jg + 1):
+            for kk in range(k):
+                rs = min(kk * L, ng)
+                run = keys[gbase + rs:gbase + rs + lens[kk]]
+                if j == 0:
+                    c = 0
+                elif j == jg:
+                    c = lens[kk]
+                else:
+                    fpos = g * k * Ls + j * G
+                    assert fpos < len(fk)
+                    v = fk[fpos]
+                    sidx = int(fi[fpos])
+                    rr = sidx // Ls
+                    kb = rr - g * k
+                    ib = (sidx - rr * Ls) * B
+                    assert 0 <= kb < k
+                    if kk == kb:
+                        c = ib
+                    elif kk < kb:
+                        c = int(np.searchsorted(run, v, side="right"))
+                    else:
+                        c = int(np.searchsorted(run, v, side="left"))
+                desc[j, kk] = c
+        doff = desc.sum(axis=1)
+        for j in range(jg):
+            seg_k, seg_i = [], []
+            for kk in range(k):
+                lo, hi = desc[j, kk], desc[j + 1, kk]
+                assert lo <= hi, "boundaries must be monotone per run"
+                base = gbase + min(kk * L, ng)
+                seg_k.append(keys[base + lo:base + hi])
+                seg_i.append(idx[base + lo:base + hi])
+            tk = np.concatenate(seg_k)
+            ti = np.concatenate(seg_i)
+            cnt = len(tk)
+            max_tile = max(max_tile, cnt)
+            assert cnt <= cap, f"tile of {cnt} keys exceeds CAP={cap} (level {level})"
+            assert cnt <= (G + k) * B
+            mk, mi = _stable_merge(tk, ti)
+            o = gbase + doff[j]
+            out_k[o:o + cnt] = mk
+            out_i[o:o + cnt] = mi
+        assert doff[jg] == ng
+    stats.setdefault("max_tile", []).append((level, max_tile))
+    stats["tile_launches"] = stats.get("tile_launches", 0) + 1
+    return out_k, out_i
+
+
+def model_sort(keys, geo):
+    """Engine::sort: base tiles of CAP, then rounds with L = CAP * K^p."""
+    n = len(keys)
+    idx = np.arange(n, dtype=np.int64)
+    stats = {}
+    k = keys.copy()
+    for tb in range(0, n, geo.cap):
+        te = min(n, tb + geo.cap)
+        k[tb:te], idx[tb:te] = _stable_merge(k[tb:te], idx[tb:te])
+    L = geo.cap
+    rounds = 0
+    while L < n:
+        k, idx = model_round(k, idx, L, geo, stats)
+        L *= geo.k
+        rounds += 1
+    stats["rounds"] = rounds
+    return k, idx, stats

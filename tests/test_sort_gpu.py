@@ -1,0 +1,241 @@
+"""GPU parity: the sm_103a library, called through its C ABI, against the oracle.
+
+Integer, float (total order) and key/value results must be bit-identical to
+std::sort / std::stable_sort (oracle/oracle.cpp).  The reference-generated
+golden set (tests/golden/ref_random_list.npz: the reference's own input
+generator and its selection-sort checker) is replayed first.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+pytestmark = pytest.mark.gpu
+
+SIGNED = {np.dtype(np.uint32): np.int32, np.dtype(np.uint64): np.int64, np.dtype(np.float32): np.int32,
+          np.dtype(np.float64): np.int64, np.dtype(np.int32): np.int32, np.dtype(np.int64): np.int64}
+SUFFIX = {np.dtype(np.int32): "i32", np.dtype(np.uint32): "u32", np.dtype(np.float32): "f32",
+          np.dtype(np.int64): "i64", np.dtype(np.uint64): "u64", np.dtype(np.float64): "f64"}
+
+
+def to_dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a).view(SIGNED[a.dtype])).cuda()
+
+
+def from_dev(t, dtype):
+    return t.cpu().numpy().view(dtype)
+
+
+def stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def gpu_sort(gms, a):
+    lib = gms.load()
+    tin = to_dev(a)
+    tout = torch.empty_like(tin)
+    fn = getattr(lib, "gms_sort_" + SUFFIX[a.dtype])
+    st = fn(tin.data_ptr(), tout.data_ptr(), a.size, 0, stream())
+    assert st == 0, lib.gms_last_error()
+    assert gms.device_status() == 0
+    return from_dev(tout, a.dtype)
+
+
+def gpu_sort_kv(gms, k, v):
+    lib = gms.load()
+    ki, vi = to_dev(k), to_dev(v.astype(np.int32))
+    ko, vo = torch.empty_like(ki), torch.empty_like(vi)
+    fn = getattr(lib, f"gms_sort_kv_{SUFFIX[k.dtype]}_i32")
+    st = fn(ki.data_ptr(), vi.data_ptr(), ko.data_ptr(), vo.data_ptr(), k.size, 0, stream())
+    assert st == 0, lib.gms_last_error()
+    assert gms.device_status() == 0
+    return from_dev(ko, k.dtype), from_dev(vo, np.int32)
+
+
+def assert_same(got, want, what=""):
+    if not np.array_equal(got.view(SIGNED[got.dtype]), want.view(SIGNED[want.dtype])):
+        d = np.nonzero(got.view(SIGNED[got.dtype]) != want.view(SIGNED[want.dtype]))[0]
+        raise AssertionError(f"{what}: {d.size} mismatches, first at {d[0]}: got {got[d[0]]} want {want[d[0]]}")
+
+
+# ---------------------------------------------------------------------------
+def test_reference_golden_inputs(gms, golden):
+    """The reference's own test inputs, sorted as its checker sorts them."""
+    for n, seed in [tuple(int(x) for x in c) for c in golden["cases"]]:
+        got = gpu_sort(gms, golden[f"in_{n}_{seed}"])
+        assert_same(got, golden[f"sorted_{n}_{seed}"], f"n={n} seed={seed}")
+
+
+def test_tile_sort_matches_square_sort_golden(gms, golden):
+    """squareSort contract with the reference's M=1024 tiles (and tail)."""
+    lib = gms.load()
+    for n, seed in [tuple(int(x) for x in c) for c in golden["cases"]]:
+        if n == 0:
+            continue
+        t = to_dev(golden[f"in_{n}_{seed}"])
+        assert lib.gms_tile_sort_i32(t.data_ptr(), n, 1024, stream()) == 0
+        assert_same(from_dev(t, np.int32), golden[f"tiles1024_{n}_{seed}"], f"n={n}")
+
+
+@pytest.mark.parametrize("tile", [1, 2, 17, 1000, 4096, 8703, 8704])
+def test_tile_sort_tiles(gms, oracle, tile):
+    lib = gms.load()
+    a = oracle.gen_i32(50001, 6, tile)
+    t = to_dev(a)
+    assert lib.gms_tile_sort_i32(t.data_ptr(), a.size, tile, stream()) == 0
+    assert_same(from_dev(t, np.int32), oracle.tile_sort(a, tile), f"tile={tile}")
+
+
+SIZES = [0, 1, 2, 3, 31, 100, 1023, 8703, 8704, 8705, 17409, 100000, 278528, 278529, 1000003, 3 * 278528 + 17]
+
+
+@pytest.mark.parametrize("n", SIZES)
+def test_sort_i32_sizes(gms, oracle, n):
+    a = oracle.gen_i32(n, 6, 1000 + n)
+    assert_same(gpu_sort(gms, a), oracle.sort(a), f"n={n}")
+
+
+@pytest.mark.parametrize("dist", range(7))
+def test_sort_i32_distributions(gms, oracle, dist):
+    n = (1 << 22) + 12345
+    a = oracle.gen_i32(n, dist, 77)
+    assert_same(gpu_sort(gms, a), oracle.sort(a), f"dist={dist}")
+
+
+def test_sort_i32_two_rounds(gms, oracle):
+    n = 9_000_001  # 2 merge rounds, recursive sample merge
+    a = oracle.gen_i32(n, 6, 5)
+    assert_same(gpu_sort(gms, a), oracle.sort(a))
+
+
+@pytest.mark.parametrize("dtype", [np.uint32, np.int64, np.uint64])
+def test_sort_integer_dtypes(gms, oracle, dtype):
+    rng = np.random.default_rng(9)
+    info = np.iinfo(dtype)
+    for n in [5, 8705, 300001, 2_500_003]:
+        a = rng.integers(info.min, info.max, n, dtype=dtype, endpoint=True)
+        assert_same(gpu_sort(gms, a), oracle.sort(a), f"{dtype} n={n}")
+
+
+def test_sort_f32_total_order(gms, oracle):
+    for n in [7, 8705, 1_000_003]:
+        a = oracle.gen_f32(n, 31 + n)
+        assert_same(gpu_sort(gms, a), oracle.sort(a), f"n={n}")
+
+
+def test_sort_f64_total_order(gms, oracle):
+    a = oracle.gen_f32(700001, 3).astype(np.float64)
+    a[::1000] = -0.0
+    bits = a.view(np.uint64)
+    bits[5::997] = np.uint64(0xFFF8000000000123)  # negative NaN with payload
+    assert_same(gpu_sort(gms, a), oracle.sort(a))
+
+
+def test_full_key_range_extremes(gms, oracle):
+    """No sentinel: INT_MAX / INT_MIN (the reference's MAXVAL) sort like any key."""
+    rng = np.random.default_rng(4)
+    a = rng.choice(np.array([2**31 - 1, -2**31, 0, -1, 1, 2**31 - 2], dtype=np.int32), 300007)
+    assert_same(gpu_sort(gms, a), oracle.sort(a))
+    b = rng.choice(np.array([2**64 - 1, 0, 2**63, 2**63 - 1], dtype=np.uint64), 100003)
+    assert_same(gpu_sort(gms, b), oracle.sort(b))
+
+
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("n", [1, 100, 8705, 300001, 2_000_003])
+def test_kv_u64_stable(gms, oracle, n):
+    k = oracle.gen_u64(n, 17 + n)
+    k[::3] = k[0]  # many ties: stability is visible in the payload
+    v = np.arange(n, dtype=np.int32)
+    gk, gv = gpu_sort_kv(gms, k, v)
+    ok, ov = oracle.sort_kv(k, v)
+    assert_same(gk, ok, "keys")
+    assert_same(gv, ov, "payload")
+
+
+@pytest.mark.parametrize("dtype", [np.int32, np.uint32, np.float32, np.int64, np.float64])
+def test_kv_other_dtypes(gms, oracle, dtype):
+    rng = np.random.default_rng(12)
+    n = 400009
+    if dtype == np.float32:
+        k = oracle.gen_f32(n, 5)
+    elif dtype == np.float64:
+        k = oracle.gen_f32(n, 6).astype(np.float64)
+    else:
+        k = rng.integers(-50 if np.dtype(dtype).kind == "i" else 0, 50, n).astype(dtype)
+    v = rng.integers(-2**31, 2**31 - 1, n, dtype=np.int64).astype(np.int32)
+    gk, gv = gpu_sort_kv(gms, k, v)
+    ok, ov = oracle.sort_kv(k, v)
+    assert_same(gk, ok, "keys")
+    assert_same(gv, ov, "payload")
+
+
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("run_len,k", [(1, 2), (1, 32), (7, 3), (100, 32), (1000, 32), (8704, 32), (5000, 7),
+                                       (100000, 4)])
+def test_merge_level(gms, oracle, run_len, k):
+    lib = gms.load()
+    n = 600011
+    a = oracle.tile_sort(oracle.gen_i32(n, 4 if k == 7 else 6, run_len), run_len)
+    t = to_dev(a)
+    o = torch.empty_like(t)
+    assert lib.gms_merge_level_i32(t.data_ptr(), o.data_ptr(), n, run_len, k, stream()) == 0, lib.gms_last_error()
+    assert gms.device_status() == 0
+    assert_same(from_dev(o, np.int32), oracle.merge_level(a, run_len, k), f"L={run_len} k={k}")
+    assert_same(from_dev(t, np.int32), a, "input untouched")
+
+
+def test_merge_level_u64(gms, oracle):
+    lib = gms.load()
+    n, L, k = 400003, 3001, 16
+    a = np.sort(oracle.gen_u64(n, 1).reshape(-1)[: n])
+    a = oracle.tile_sort(oracle.gen_u64(n, 2), L)
+    t = to_dev(a)
+    o = torch.empty_like(t)
+    assert lib.gms_merge_level_u64(t.data_ptr(), o.data_ptr(), n, L, k, stream()) == 0
+    assert_same(from_dev(o, np.uint64), oracle.merge_level(a, L, k))
+
+
+@pytest.mark.parametrize("size,k", [(1000, 8), (50000, 32), (100, 3)])
+def test_find_partitions(gms, oracle, size, k):
+    lib = gms.load()
+    task = oracle.tile_sort(oracle.gen_i32(size * k - 5, 4, size), size)
+    mergers = 13
+    ranks = np.array([m * task.size // mergers for m in range(mergers + 1)] + [1, task.size - 1], dtype=np.int64)
+    tt, tr = to_dev(task), torch.from_numpy(ranks).cuda()
+    out = torch.empty((ranks.size, k), dtype=torch.int64, device="cuda")
+    st = lib.gms_find_partitions_i32(tt.data_ptr(), size, k, task.size, tr.data_ptr(), ranks.size, out.data_ptr(),
+                                     stream())
+    assert st == 0, lib.gms_last_error()
+    assert np.array_equal(out.cpu().numpy(), oracle.find_partitions(task, size, k, ranks))
+
+
+# ---------------------------------------------------------------------------
+def test_deterministic_repeats(gms, oracle):
+    a = oracle.gen_i32(2_000_003, 5, 3)
+    first = gpu_sort(gms, a)
+    for _ in range(3):
+        assert_same(gpu_sort(gms, a), first)
+
+
+def test_host_entry_point(gms, oracle):
+    lib = gms.load()
+    a = oracle.gen_i32(1_000_003, 0, 8)
+    hin = torch.from_numpy(a.copy()).pin_memory()
+    hout = torch.empty_like(hin).pin_memory()
+    assert lib.gms_sort_host_i32(hin.data_ptr(), hout.data_ptr(), a.size, stream()) == 0
+    assert_same(hout.numpy(), oracle.sort(a))
+
+
+def test_invalid_arguments(gms):
+    lib = gms.load()
+    t = torch.zeros(16, dtype=torch.int32, device="cuda")
+    assert lib.gms_sort_i32(t.data_ptr(), t.data_ptr(), -1, 0, stream()) == 1
+    assert lib.gms_sort_i32(None, t.data_ptr(), 5, 0, stream()) == 1
+    assert lib.gms_merge_level_i32(t.data_ptr(), t.data_ptr(), 16, 4, 1, stream()) == 1
+    assert lib.gms_merge_level_i32(t.data_ptr(), t.data_ptr(), 16, 4, 33, stream()) == 1
+    assert lib.gms_tile_sort_i32(t.data_ptr(), 16, 0, stream()) == 1
+    assert lib.gms_tile_sort_i32(t.data_ptr(), 16, 8705, stream()) == 1
+    assert b"n" in lib.gms_last_error() or lib.gms_last_error() != b""
+    assert lib.gms_sort_i32(t.data_ptr(), t.data_ptr(), 0, 0, stream()) == 0
