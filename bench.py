@@ -1,0 +1,362 @@
+"""Benchmark of the GB300 multiway mergesort: int32 N=2^28 keys.
+
+One step = one full sort of N = 2^28 int32 keys drawn uniformly from
+[0, 2^31-1) with a fixed seed (the reference's scale configuration), through
+the C ABI (gms_sort_i32).  Each timed step sorts its own fresh copy of the
+input (1 GiB per copy, far above the 129 MB L2), so no step sees a warm cache.
+
+  value       Gkeys/s, device-resident input, the K steps timed with CUDA
+              events between a barrier + synchronize on both sides
+  e2e         Gkeys/s through gms_sort_host_i32 from pinned host memory:
+              H2D copy + sort + D2H copy + stream wait, every step
+  roofline    the dominant kernel's algorithmic bytes per launch / its mean
+              launch time, both measured live in the timed region, against the
+              measured HBM copy bandwidth
+  cpu_baseline std::sort (libstdc++ parallel mode, all host threads) on a
+              bounded sample of the same workload (oracle, CPU only)
+
+`--impl reference` times the CPU implementation (the oracle's std::sort with
+every host thread): the reference ships no CPU sort of its own.
+Multi-GPU (torchrun): every rank sorts its own replica; no collective on the
+data path ("replicas only"); value = keys of all ranks / max time over ranks.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+N_DEFAULT = 1 << 28
+SEED = 1
+PEAK_FALLBACK_GBS = 6800.0
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return PEAK_FALLBACK_GBS, "fallback"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi samples every 200 ms while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.gpu)], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) >= 9:
+                    rows.append(f)
+        except OSError:
+            pass
+        finally:
+            if self.path and os.path.exists(self.path):
+                os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        mx = [num(r[2]) for r in rows if num(r[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        pw = [num(r[3]) for r in rows if num(r[3]) is not None]
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows), "power_w_max": max(pw) if pw else None}
+
+
+def cpu_baseline(orc, n_sample, reps=3):
+    """std::sort, libstdc++ parallel mode, every host thread, on n_sample keys."""
+    import numpy as np
+
+    threads = os.cpu_count() or 1
+    a = orc.gen_i32(n_sample, 0, SEED)
+    best = None
+    for _ in range(reps):
+        b = a.copy()
+        t0 = time.perf_counter()
+        used = orc.lib.gmo_par_sort_i32(ctypes.c_void_p(b.ctypes.data), b.size, threads)
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
+    assert np.all(b[1:] >= b[:-1])
+    return {"value": round(n_sample / best / 1e9, 4), "unit": "Gkeys/s", "cores": int(used),
+            "kind": "port", "sample": f"{n_sample} int32 keys of the same distribution, std::sort "
+            f"(__gnu_parallel) on {int(used)} threads, best of {reps}"}
+
+
+def run_reference(args):
+    """CPU arm: the oracle's std::sort with every host thread."""
+    import numpy as np
+    from conftest import Oracle
+
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    orc = Oracle()
+    n = args.n
+    threads = os.cpu_count() or 1
+    src = orc.gen_i32(n, 0, SEED)
+    # one untimed probe decides whether a step can take the full workload
+    probe = src.copy()
+    t0 = time.perf_counter()
+    orc.lib.gmo_par_sort_i32(ctypes.c_void_p(probe.ctypes.data), probe.size, threads)
+    per_full = time.perf_counter() - t0
+    budget_s = 150.0
+    sample = n if per_full * (args.steps + args.warmup) <= budget_s else max(1 << 20, n >> 2)
+    work = src[:sample]
+    times = []
+    for i in range(args.warmup + args.steps):
+        b = work.copy()
+        t0 = time.perf_counter()
+        used = orc.lib.gmo_par_sort_i32(ctypes.c_void_p(b.ctypes.data), b.size, threads)
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            times.append(dt)
+    assert np.all(b[1:] >= b[:-1])
+    tot = sum(times)
+    value = sample * len(times) / tot / 1e9
+    line = {
+        "metric": "Gkeys/s int32 N=2^28", "value": round(value, 4), "unit": "Gkeys/s", "impl": "reference",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(tot / len(times) * 1e3, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic: uniform int32 in [0, 2^31-1), mt19937_64 seed 1",
+        "config": {"workload": f"int32 N={n} uniform sort on the host CPU", "n": n, "sample": sample},
+        "cpu_baseline": {"value": round(value, 4), "unit": "Gkeys/s", "cores": int(used), "kind": "port",
+                         "sample": f"{sample} keys per step, std::sort (__gnu_parallel) on {int(used)} threads; "
+                                   "the reference has no CPU sort, so this is the oracle's std::sort"},
+        "e2e": {"value": round(value, 4), "unit": "Gkeys/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    from conftest import Oracle, load_gms_module
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    gms = load_gms_module()
+    gms.build()
+    lib = gms.load()
+    orc = Oracle()
+    n = args.n
+    stream = torch.cuda.current_stream()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+
+    src_h = orc.gen_i32(n, 0, SEED + rank)
+    src = torch.from_numpy(src_h).cuda()
+    ncopies = max(args.steps, args.warmup)
+    inputs = [torch.empty_like(src) for _ in range(ncopies)]
+    out = torch.empty_like(src)
+    assert lib.gms_reserve(0, 0, n, sp) == 0
+
+    def refill(k):
+        for t in inputs[:k]:
+            t.copy_(src)
+        torch.cuda.synchronize()
+
+    def sort_one(t):
+        rc = lib.gms_sort_i32(t.data_ptr(), out.data_ptr(), n, 0, sp)
+        if rc != 0:
+            raise RuntimeError(lib.gms_last_error().decode())
+
+    # warm-up
+    refill(args.warmup)
+    for i in range(args.warmup):
+        sort_one(inputs[i])
+    torch.cuda.synchronize()
+    # correctness of the last warm-up result (full-size, bit-exact vs torch.sort)
+    ok = bool(torch.equal(out, torch.sort(src)[0]))
+    refill(args.steps)
+
+    # ---- timed region ----
+    lib.gms_timing_reset()
+    lib.gms_timing_enable(1)
+    launches0 = lib.gms_launch_count()
+    gpu_index = local
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+    if vis:
+        try:
+            gpu_index = int(vis.split(",")[local])
+        except ValueError:
+            pass
+    with ClockSampler(gpu_index) as clk:
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for i in range(args.steps):
+            sort_one(inputs[i])
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+    lib.gms_timing_enable(0)
+    launches = lib.gms_launch_count() - launches0
+    ms_total = e0.elapsed_time(e1)
+    per_kernel = gms.timing_collect()
+    if dist:
+        t = torch.tensor([ms_total], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_total = float(t.item())
+    ms_step = ms_total / args.steps
+    value = n * ws * args.steps / (ms_total * 1e-3) / 1e9
+
+    # ---- end to end through the C ABI with host buffers ----
+    hin = torch.from_numpy(src_h).pin_memory()
+    hout = torch.empty_like(hin).pin_memory()
+    for _ in range(1):
+        assert lib.gms_sort_host_i32(hin.data_ptr(), hout.data_ptr(), n, sp) == 0
+    e2e_steps = min(args.steps, 5)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        rc = lib.gms_sort_host_i32(hin.data_ptr(), hout.data_ptr(), n, sp)
+        assert rc == 0, lib.gms_last_error()
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_ok = bool(np.array_equal(hout.numpy(), out.cpu().numpy()))
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return 0
+
+    # ---- roofline of the dominant kernel ----
+    peak, peak_kind = peaks()
+    rounds = int(lib.gms_rounds(0, 0, n))
+    passes = 1 + rounds
+    bytes_per_pass = 2 * n * 4
+    dom = max(per_kernel.items(), key=lambda kv: kv[1][0])
+    dom_name, (dom_ms, dom_launches) = dom
+    dom_avg_ms = dom_ms / max(dom_launches, 1)
+    achieved = bytes_per_pass / (dom_avg_ms * 1e-3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        traffic = json.load(open(tpath)).get(dom_name)
+    sort_bytes = bytes_per_pass * passes
+    line = {
+        "metric": "Gkeys/s int32 N=2^28",
+        "value": round(value, 3),
+        "unit": "Gkeys/s",
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms_step, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "int32",
+        "data": "synthetic: uniform int32 in [0, 2^31-1), mt19937_64 seed 1 (+rank)",
+        "config": {
+            "workload": f"multimergesort int32 N={n} uniform, one full sort per step",
+            "n": n, "rounds": rounds, "passes": passes, "base_tile": int(lib.gms_base_tile(0, 0)), "k": 32,
+            "sample_block": 32, "parallelism": "replicas" if ws > 1 else "single",
+            "l2": "each step sorts its own 1 GiB input copy (> 129 MB L2)",
+            "correct": ok and e2e_ok,
+        },
+        "roofline": {
+            "bound": "hbm", "kernel": dom_name, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+            "bytes_per_launch": bytes_per_pass, "mean_launch_ms": round(dom_avg_ms, 4),
+            "traffic": traffic,
+            "sort_frac": round(sort_bytes / (ms_step * 1e-3) / 1e9 / peak, 4),
+        },
+        "per_kernel_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in per_kernel.items() if v[1]},
+        "e2e": {"value": round(n * ws / e2e_s / 1e9, 3), "unit": "Gkeys/s", "h2d_bytes_per_step": n * 4,
+                "d2h_bytes_per_step": n * 4, "ms_per_step": round(e2e_s * 1e3, 3)},
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(orc, min(n, 1 << 26))
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.steps < 1 or args.warmup < 0:
+        ap.error("steps >= 1, warmup >= 0")
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

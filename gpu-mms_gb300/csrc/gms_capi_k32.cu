@@ -86,10 +86,12 @@ int gms_find_partitions_i32(const int32_t* task, int64_t size, int k, int64_t ta
     if (e != cudaSuccess) return cuda_error(e, "find_partitions merge");
   }
   const int64_t threads = nranks * 32;
+  gms::hook_before(gms::KC_CORANK, st);
   gms::corank_kernel<uint32_t, gms::KeyLess, gms::SignFlip32>
       <<<(unsigned)gms::ceil_div(threads, 256), 256, 0, st>>>((const uint32_t*)task, mk, mi, size, k, task_size, ranks,
                                                                nranks, out);
   e = cudaGetLastError();
+  gms::hook_after(gms::KC_CORANK, st);
   return e == cudaSuccess ? GMS_OK : cuda_error(e, "corank_kernel");
 }
 

@@ -74,6 +74,52 @@ void* cache_get(int tag, size_t bytes, cudaStream_t st, int* status) {
   return p;
 }
 
+// ---- launch counting and live kernel timing ----
+namespace {
+struct TimedLaunch {
+  int kc;
+  cudaEvent_t a, b;
+};
+std::mutex g_prof_mu;
+long long g_launches[gms::KC_COUNT] = {0};
+int g_timing = 0;
+std::vector<TimedLaunch> g_pending;
+std::vector<cudaEvent_t> g_event_pool;
+double g_ms[gms::KC_COUNT] = {0};
+long long g_timed[gms::KC_COUNT] = {0};
+cudaEvent_t g_open[gms::KC_COUNT];
+
+cudaEvent_t pool_event() {
+  if (!g_event_pool.empty()) {
+    cudaEvent_t e = g_event_pool.back();
+    g_event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+void before_launch(int kc, cudaStream_t st) {
+  std::lock_guard<std::mutex> g(g_prof_mu);
+  if (!g_timing) return;
+  g_open[kc] = pool_event();
+  cudaEventRecord(g_open[kc], st);
+}
+void after_launch(int kc, cudaStream_t st) {
+  std::lock_guard<std::mutex> g(g_prof_mu);
+  g_launches[kc]++;
+  if (!g_timing) return;
+  cudaEvent_t b = pool_event();
+  cudaEventRecord(b, st);
+  g_pending.push_back(TimedLaunch{kc, g_open[kc], b});
+}
+gms::Hooks g_hook_table{before_launch, after_launch};
+struct InstallHooks {
+  InstallHooks() { gms::g_hooks = &g_hook_table; }
+} g_install_hooks;
+}  // namespace
+
 }  // namespace gms_capi
 
 using namespace gms_capi;
@@ -106,6 +152,49 @@ void gms_release_workspaces(void) {
     cudaSetDevice(cur);
   }
   g_slots.clear();
+}
+
+long long gms_launch_count(void) {
+  std::lock_guard<std::mutex> g(g_prof_mu);
+  long long t = 0;
+  for (int i = 0; i < gms::KC_COUNT; ++i) t += g_launches[i];
+  return t;
+}
+
+int gms_timing_enable(int on) {
+  std::lock_guard<std::mutex> g(g_prof_mu);
+  g_timing = on ? 1 : 0;
+  return GMS_OK;
+}
+
+int gms_timing_collect(double* ms, long long* launches, int nclasses) {
+  clear_error();
+  std::lock_guard<std::mutex> g(g_prof_mu);
+  for (const TimedLaunch& t : g_pending) {
+    float f = 0.f;
+    cudaError_t e = cudaEventSynchronize(t.b);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&f, t.a, t.b);
+    if (e != cudaSuccess) return cuda_error(e, "cudaEventElapsedTime");
+    g_ms[t.kc] += f;
+    g_timed[t.kc] += 1;
+    g_event_pool.push_back(t.a);
+    g_event_pool.push_back(t.b);
+  }
+  g_pending.clear();
+  for (int i = 0; i < nclasses && i < gms::KC_COUNT; ++i) {
+    if (ms) ms[i] = g_ms[i];
+    if (launches) launches[i] = g_timed[i];
+  }
+  return GMS_OK;
+}
+
+int gms_timing_reset(void) {
+  std::lock_guard<std::mutex> g(g_prof_mu);
+  for (int i = 0; i < gms::KC_COUNT; ++i) {
+    g_ms[i] = 0;
+    g_timed[i] = 0;
+  }
+  return GMS_OK;
 }
 
 int64_t gms_max_tile(void) { return (int64_t)kNT * kItems; }

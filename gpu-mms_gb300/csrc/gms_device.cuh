@@ -35,10 +35,10 @@ struct HasVal<NoVal> {
 // Codecs map a user key's bit pattern to an unsigned key whose `<` order is
 // the user order, and back.  The first pass encodes on load, the last pass
 // decodes on store; every pass in between compares plain unsigned integers.
-template <class K>
+template <class KeyT>
 struct IdentityCodec {
-  static __device__ __forceinline__ K enc(K x) { return x; }
-  static __device__ __forceinline__ K dec(K x) { return x; }
+  static __device__ __forceinline__ KeyT enc(KeyT x) { return x; }
+  static __device__ __forceinline__ KeyT dec(KeyT x) { return x; }
 };
 // two's-complement order -> unsigned order
 struct SignFlip32 {
@@ -69,8 +69,8 @@ struct FloatOrder64 {
 
 // Default strict weak order on the stored keys.
 struct KeyLess {
-  template <class K>
-  __device__ __forceinline__ bool operator()(const K& a, const K& b) const {
+  template <class KeyT>
+  __device__ __forceinline__ bool operator()(const KeyT& a, const KeyT& b) const {
     return a < b;
   }
 };
@@ -81,11 +81,11 @@ struct KeyLess {
 
 // Compare-exchange: afterwards a <= b.  Not stable (used where equivalent keys
 // are bit-identical).
-template <class K, class Cmp>
-__device__ __forceinline__ void cas(K& a, K& b, Cmp cmp) {
+template <class KeyT, class Cmp>
+__device__ __forceinline__ void cas(KeyT& a, KeyT& b, Cmp cmp) {
   const bool sw = cmp(b, a);
-  const K lo = sw ? b : a;
-  const K hi = sw ? a : b;
+  const KeyT lo = sw ? b : a;
+  const KeyT hi = sw ? a : b;
   a = lo;
   b = hi;
 }
@@ -126,8 +126,8 @@ struct Batcher {
   static constexpr NetTable table = batcher_table(N);
 };
 
-template <int N, int C, class K, class Cmp>
-__device__ __forceinline__ void network_apply(K (&r)[N], Cmp cmp) {
+template <int N, int C, class KeyT, class Cmp>
+__device__ __forceinline__ void network_apply(KeyT (&r)[N], Cmp cmp) {
   if constexpr (C < Batcher<N>::table.n) {
     constexpr int ia = Batcher<N>::table.a[C];
     constexpr int ib = Batcher<N>::table.b[C];
@@ -136,23 +136,23 @@ __device__ __forceinline__ void network_apply(K (&r)[N], Cmp cmp) {
   }
 }
 
-template <int N, class K, class Cmp>
-__device__ __forceinline__ void network_sort(K (&r)[N], Cmp cmp) {
+template <int N, class KeyT, class Cmp>
+__device__ __forceinline__ void network_sort(KeyT (&r)[N], Cmp cmp) {
   network_apply<N, 0>(r, cmp);
 }
 
 // Odd-even transposition sort: only adjacent keys are exchanged, and only when
 // strictly out of order, so equal keys keep their order (stable).  Carries a
 // payload along.
-template <int N, class K, class V, class Cmp>
-__device__ __forceinline__ void transposition_sort(K (&r)[N], V (&v)[N], Cmp cmp) {
+template <int N, class KeyT, class V, class Cmp>
+__device__ __forceinline__ void transposition_sort(KeyT (&r)[N], V (&v)[N], Cmp cmp) {
 #pragma unroll
   for (int round = 0; round < N; ++round) {
 #pragma unroll
     for (int i = round & 1; i + 1 < N; i += 2) {
       const bool sw = cmp(r[i + 1], r[i]);
-      const K klo = sw ? r[i + 1] : r[i];
-      const K khi = sw ? r[i] : r[i + 1];
+      const KeyT klo = sw ? r[i + 1] : r[i];
+      const KeyT khi = sw ? r[i] : r[i + 1];
       r[i] = klo;
       r[i + 1] = khi;
       if constexpr (HasVal<V>::value) {
@@ -168,8 +168,8 @@ __device__ __forceinline__ void transposition_sort(K (&r)[N], V (&v)[N], Cmp cmp
 // ---------------------------------------------------------------------------
 // Merge path: number of elements of `a` among the first `diag` outputs of the
 // stable merge of a and b (a wins ties).
-template <class K, class Cmp>
-__device__ __forceinline__ int merge_path(const K* a, int na, const K* b, int nb, int diag, Cmp cmp) {
+template <class KeyT, class Cmp>
+__device__ __forceinline__ int merge_path(const KeyT* a, int na, const KeyT* b, int nb, int diag, Cmp cmp) {
   int lo = diag - nb > 0 ? diag - nb : 0;
   int hi = diag < na ? diag : na;
   while (lo < hi) {
@@ -187,9 +187,9 @@ __device__ __forceinline__ int merge_path(const K* a, int na, const K* b, int nb
 // shared-memory tile of `cap` keys (cap a multiple of 2*rl or the tail run
 // shorter).  Thread `t` produces outputs [t*ITEMS, t*ITEMS + ITEMS) into
 // registers.  ITEMS divides rl, so a thread never straddles two pairs.
-template <int ITEMS, class K, class V, class Cmp>
-__device__ __forceinline__ void merge_level_regular(const K* sk, const V* sv, int cap, int rl, int s,
-                                                    K (&ok)[ITEMS], V (&ov)[ITEMS], Cmp cmp) {
+template <int ITEMS, class KeyT, class V, class Cmp>
+__device__ __forceinline__ void merge_level_regular(const KeyT* sk, const V* sv, int cap, int rl, int s,
+                                                    KeyT (&ok)[ITEMS], V (&ov)[ITEMS], Cmp cmp) {
   const int ps = (s / (2 * rl)) * (2 * rl);
   const int pm = min(ps + rl, cap);
   const int pe = min(ps + 2 * rl, cap);
@@ -197,8 +197,8 @@ __device__ __forceinline__ void merge_level_regular(const K* sk, const V* sv, in
   const int ia = merge_path(sk + ps, pm - ps, sk + pm, pe - pm, diag, cmp);
   int xa = ps + ia;
   int xb = pm + (diag - ia);
-  K ka = sk[xa];
-  K kb = sk[xb];
+  KeyT ka = sk[xa];
+  KeyT kb = sk[xb];
 #pragma unroll
   for (int i = 0; i < ITEMS; ++i) {
     const bool ta = (xb >= pe) || ((xa < pm) && !cmp(kb, ka));
@@ -219,9 +219,9 @@ __device__ __forceinline__ void merge_level_regular(const K* sk, const V* sv, in
 // [pre[p*span], pre[p*span+span/2]) and [pre[p*span+span/2], pre[p*span+span])
 // are merged.  Runs may be empty; a thread whose ITEMS outputs straddle the end
 // of one pair continues with the next non-empty pair.
-template <int ITEMS, class K, class V, class Cmp>
-__device__ __forceinline__ void merge_level_var(const K* sk, const V* sv, const int* pre, int nk, int span,
-                                                int s, int e, K (&ok)[ITEMS], V (&ov)[ITEMS], Cmp cmp) {
+template <int ITEMS, class KeyT, class V, class Cmp>
+__device__ __forceinline__ void merge_level_var(const KeyT* sk, const V* sv, const int* pre, int nk, int span,
+                                                int s, int e, KeyT (&ok)[ITEMS], V (&ov)[ITEMS], Cmp cmp) {
   const int npairs = (nk + span - 1) / span;
   // largest pair index whose start is <= s
   int lo = 0, hi = npairs - 1;
@@ -241,8 +241,8 @@ __device__ __forceinline__ void merge_level_var(const K* sk, const V* sv, const 
   const int ia = merge_path(sk + ps, pm - ps, sk + pm, pe - pm, diag, cmp);
   int xa = ps + ia;
   int xb = pm + (diag - ia);
-  K ka = sk[xa];
-  K kb = sk[xb];
+  KeyT ka = sk[xa];
+  KeyT kb = sk[xb];
 #pragma unroll
   for (int i = 0; i < ITEMS; ++i) {
     if (s + i < e) {
@@ -284,21 +284,21 @@ __device__ __forceinline__ void merge_level_var(const K* sk, const V* sv, const 
 // Largest element (under cmp) across the block; every thread gets it.
 // `scratch` holds NT keys.  Shared-memory tree, so any copyable key type works
 // (no shuffle of user types).
-template <int NT, class K, class Cmp>
-__device__ __forceinline__ K block_max(K x, K* scratch, Cmp cmp) {
+template <int NT, class KeyT, class Cmp>
+__device__ __forceinline__ KeyT block_max(KeyT x, KeyT* scratch, Cmp cmp) {
   const int t = threadIdx.x;
   scratch[t] = x;
   __syncthreads();
 #pragma unroll
   for (int s = NT / 2; s > 0; s >>= 1) {
     if (t < s) {
-      const K a = scratch[t];
-      const K b = scratch[t + s];
+      const KeyT a = scratch[t];
+      const KeyT b = scratch[t + s];
       scratch[t] = cmp(a, b) ? b : a;
     }
     __syncthreads();
   }
-  const K m = scratch[0];
+  const KeyT m = scratch[0];
   __syncthreads();
   return m;
 }

@@ -22,10 +22,10 @@ namespace gms {
 enum TileMode : int { MODE_BASE = 0, MODE_GROUP = 1, MODE_TILE = 2 };
 
 // Arguments of one launch of tile_kernel.
-template <class K, class V>
+template <class KeyT, class V>
 struct TileArgs {
-  const K* in;
-  K* out;
+  const KeyT* in;
+  KeyT* out;
   const V* vin;
   V* vout;
   int64_t n;      // elements in the array
@@ -39,7 +39,7 @@ struct TileArgs {
   int64_t tiles_last;  // tiles of the last group
   int64_t groups;
   // block sample of the output runs (for the next round); null if unused
-  K* sample_out;
+  KeyT* sample_out;
   int64_t out_run_len;     // length of an output run
   int64_t sample_run_len;  // ceil(out_run_len / sample_b)
   int sample_b;
@@ -52,10 +52,10 @@ struct TileArgs {
 // Bits of the device status word.
 enum DeviceStatus : int { DEV_TILE_OVERFLOW = 1, DEV_BAD_SEGMENT = 2 };
 
-template <class K, class V, int CAP>
+template <class KeyT, class V, int CAP>
 struct TileSmemLayout {
   static constexpr bool kHasVal = HasVal<V>::value;
-  static constexpr size_t key_bytes = ((sizeof(K) * (CAP + 1) + 15) / 16) * 16;
+  static constexpr size_t key_bytes = ((sizeof(KeyT) * (CAP + 1) + 15) / 16) * 16;
   static constexpr size_t val_bytes = kHasVal ? ((sizeof(V) * (CAP + 1) + 15) / 16) * 16 : 0;
   static constexpr int kMaxK = 32;
   static constexpr size_t pre_bytes = 16 * ((sizeof(int) * (kMaxK + 1) + 15) / 16);
@@ -65,12 +65,12 @@ struct TileSmemLayout {
 
 __device__ __forceinline__ int64_t min64(int64_t a, int64_t b) { return a < b ? a : b; }
 
-template <class Codec, class K>
-__device__ __forceinline__ K maybe_enc(K x, int on) {
+template <class Codec, class KeyT>
+__device__ __forceinline__ KeyT maybe_enc(KeyT x, int on) {
   return on ? Codec::enc(x) : x;
 }
-template <class Codec, class K>
-__device__ __forceinline__ K maybe_dec(K x, int on) {
+template <class Codec, class KeyT>
+__device__ __forceinline__ KeyT maybe_dec(KeyT x, int on) {
   return on ? Codec::dec(x) : x;
 }
 
@@ -85,13 +85,13 @@ __device__ __forceinline__ K maybe_dec(K x, int on) {
 //   MODE_TILE : CTA merges one tile of a group whose runs are cut by `desc`.
 // STABLE: equivalent keys keep their input order (used for key/value sorts and
 // for user comparators whose equivalent keys may differ in their bits).
-template <class K, class V, class Cmp, class Codec, int MODE, bool STABLE, int NT, int ITEMS>
-__global__ void __launch_bounds__(NT) tile_kernel(TileArgs<K, V> a) {
+template <class KeyT, class V, class Cmp, class Codec, int MODE, bool STABLE, int NT, int ITEMS>
+__global__ void __launch_bounds__(NT) tile_kernel(TileArgs<KeyT, V> a) {
   constexpr int CAP = NT * ITEMS;
   constexpr bool kHasVal = HasVal<V>::value;
-  using L = TileSmemLayout<K, V, CAP>;
+  using L = TileSmemLayout<KeyT, V, CAP>;
   extern __shared__ __align__(16) unsigned char smem[];
-  K* sk = reinterpret_cast<K*>(smem);
+  KeyT* sk = reinterpret_cast<KeyT*>(smem);
   V* sv = reinterpret_cast<V*>(smem + L::key_bytes);
   int* pre = reinterpret_cast<int*>(smem + L::key_bytes + L::val_bytes);
   int64_t* gs = reinterpret_cast<int64_t*>(smem + L::key_bytes + L::val_bytes + L::pre_bytes);
@@ -104,7 +104,7 @@ __global__ void __launch_bounds__(NT) tile_kernel(TileArgs<K, V> a) {
   int cnt;            // keys in this tile
   int nk = 1;         // runs in the tile (GROUP/TILE)
 
-  K ok[ITEMS];
+  KeyT ok[ITEMS];
   V ov[ITEMS];
 
   if constexpr (MODE == MODE_BASE) {
@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(NT) tile_kernel(TileArgs<K, V> a) {
     run_base = base;
     run_index = blockIdx.x;
     // Coalesced striped load: register i of thread t holds element t + i*NT.
-    K r[ITEMS];
+    KeyT r[ITEMS];
     V rv[ITEMS];
     if constexpr (STABLE) {
       // Stable: each thread must own a contiguous chunk of the input, so the
@@ -136,7 +136,7 @@ __global__ void __launch_bounds__(NT) tile_kernel(TileArgs<K, V> a) {
         if constexpr (kHasVal) rv[i] = sv[p < cnt ? p : 0];
       }
       if (cnt < CAP) {
-        K m = r[0];
+        KeyT m = r[0];
 #pragma unroll
         for (int i = 1; i < ITEMS; ++i) {
           if (tid * ITEMS + i < cnt) m = cmp(m, r[i]) ? r[i] : m;
@@ -157,7 +157,7 @@ __global__ void __launch_bounds__(NT) tile_kernel(TileArgs<K, V> a) {
         if (p < cnt) r[i] = maybe_enc<Codec>(a.in[base + p], a.enc_on_load);
       }
       if (cnt < CAP) {
-        K m = r[0];
+        KeyT m = r[0];
         if (tid >= cnt) m = maybe_enc<Codec>(a.in[base], a.enc_on_load);
 #pragma unroll
         for (int i = 1; i < ITEMS; ++i) {
@@ -204,7 +204,7 @@ __global__ void __launch_bounds__(NT) tile_kernel(TileArgs<K, V> a) {
       cnt = (int)ng;
       nk = a.k;
       if (tid <= nk) pre[tid] = (int)min64((int64_t)tid * a.L, ng);
-      const K* src = a.in + gbase;
+      const KeyT* src = a.in + gbase;
       for (int p = tid; p < cnt; p += NT) {
         sk[p] = maybe_enc<Codec>(src[p], a.enc_on_load);
         if constexpr (kHasVal) sv[p] = a.gen_index ? (V)(gbase + p) : a.vin[gbase + p];
@@ -310,8 +310,8 @@ __global__ void __launch_bounds__(NT) tile_kernel(TileArgs<K, V> a) {
 // order by binary search over run k.  Between two boundaries every run
 // contributes at most (its blocks in that stretch of F + 1) blocks, so a tile
 // holds at most (G + K) * B keys.
-template <class K, class Cmp, class Codec>
-__global__ void __launch_bounds__(256) splitter_kernel(const K* __restrict__ data, const K* __restrict__ fkeys,
+template <class KeyT, class Cmp, class Codec>
+__global__ void __launch_bounds__(256) splitter_kernel(const KeyT* __restrict__ data, const KeyT* __restrict__ fkeys,
                                                         const uint32_t* __restrict__ fidx, int64_t n, int64_t L,
                                                         int k, int64_t sample_run_len, int sample_b, int64_t G,
                                                         int64_t tiles_full, int64_t tiles_last, int64_t groups,
@@ -339,7 +339,7 @@ __global__ void __launch_bounds__(256) splitter_kernel(const K* __restrict__ dat
       c = len;
     } else {
       const int64_t fpos = g * (int64_t)k * sample_run_len + j * G;
-      const K v = fkeys[fpos];
+      const KeyT v = fkeys[fpos];
       const int64_t sidx = (int64_t)fidx[fpos];
       const int64_t run = sidx / sample_run_len;
       const int64_t kb = run - g * k;
@@ -347,7 +347,7 @@ __global__ void __launch_bounds__(256) splitter_kernel(const K* __restrict__ dat
       if (lane == kb) {
         c = ib;
       } else {
-        const K* r = data + gbase + rs;
+        const KeyT* r = data + gbase + rs;
         int64_t lo = 0, hi = len;
         if (lane < kb) {
           // keys <= v come first (earlier run wins ties)
@@ -377,8 +377,8 @@ __global__ void __launch_bounds__(256) splitter_kernel(const K* __restrict__ dat
 // ---------------------------------------------------------------------------
 // Block sample of a sample: out[r*out_run + b] = in[r*in_run + b*B] for every
 // run r and every b < ceil(len_r / B).
-template <class K, class Codec>
-__global__ void gather_sample_kernel(const K* __restrict__ in, K* __restrict__ out, int64_t n_in, int64_t in_run,
+template <class KeyT, class Codec>
+__global__ void gather_sample_kernel(const KeyT* __restrict__ in, KeyT* __restrict__ out, int64_t n_in, int64_t in_run,
                                      int64_t out_run, int b_step, int64_t n_out_slots, int enc) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n_out_slots) return;
@@ -393,8 +393,8 @@ __global__ void gather_sample_kernel(const K* __restrict__ in, K* __restrict__ o
 // merged with its origin index.  Lane k counts the keys of run k that precede
 // or equal the rank-th smallest element (stable order).  Mirrors the contract
 // of findPartitions (warp-partition.hxx:488-532) for caller-chosen ranks.
-template <class K, class Cmp, class Codec>
-__global__ void corank_kernel(const K* __restrict__ task, const K* __restrict__ merged,
+template <class KeyT, class Cmp, class Codec>
+__global__ void corank_kernel(const KeyT* __restrict__ task, const KeyT* __restrict__ merged,
                               const uint32_t* __restrict__ origin, int64_t size, int k, int64_t task_size,
                               const int64_t* __restrict__ ranks, int64_t nranks, int64_t* __restrict__ out) {
   const Cmp cmp;
@@ -408,13 +408,13 @@ __global__ void corank_kernel(const K* __restrict__ task, const K* __restrict__ 
     const int64_t re = min64((int64_t)(kk + 1) * size, task_size);
     int64_t c = 0;
     if (r > 0) {
-      const K v = merged[r - 1];
+      const KeyT v = merged[r - 1];
       const int64_t o = (int64_t)origin[r - 1];
       const int64_t kb = o / size;
       if (kk == kb) {
         c = o - kb * size + 1;
       } else {
-        const K* run = task + rs;
+        const KeyT* run = task + rs;
         int64_t lo = 0, hi = re - rs;
         if (kk < kb) {
           while (lo < hi) {

@@ -31,6 +31,33 @@ namespace gms {
 
 constexpr int kMaxLevels = 8;
 
+// Kernel classes for live timing and launch counting.
+enum KernelClass : int {
+  KC_BASE = 0,          // tile_kernel<MODE_BASE>: base-case tile sort
+  KC_MERGE = 1,         // tile_kernel<GROUP/TILE> on the data (one K-way round)
+  KC_SAMPLE_MERGE = 2,  // tile_kernel<GROUP/TILE> on block samples
+  KC_SPLIT = 3,         // splitter_kernel
+  KC_GATHER = 4,        // gather_sample_kernel
+  KC_CORANK = 5,        // corank_kernel
+  KC_COUNT = 6
+};
+
+// Optional instrumentation.  The C-ABI library installs hooks that count
+// launches and, when timing is on, bracket each launch with CUDA events on the
+// launching stream.  Code that includes these headers directly (the drop-in
+// template) has no hooks installed.
+struct Hooks {
+  void (*before)(int kc, cudaStream_t st);
+  void (*after)(int kc, cudaStream_t st);
+};
+inline Hooks* g_hooks = nullptr;
+inline void hook_before(int kc, cudaStream_t st) {
+  if (g_hooks) g_hooks->before(kc, st);
+}
+inline void hook_after(int kc, cudaStream_t st) {
+  if (g_hooks) g_hooks->after(kc, st);
+}
+
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
 // Tunables of one sort (the autotuner picks these; defaults below).
@@ -48,12 +75,12 @@ struct WsLayout {
   int depth = 0;
 };
 
-template <class K>
+template <class KeyT>
 struct WsPtrs {
   int* err = nullptr;  // device status word (first 256 bytes of the scratch)
-  K* s1[2] = {nullptr, nullptr};
-  K* s[kMaxLevels] = {nullptr};
-  K* fk[kMaxLevels] = {nullptr};
+  KeyT* s1[2] = {nullptr, nullptr};
+  KeyT* s[kMaxLevels] = {nullptr};
+  KeyT* fk[kMaxLevels] = {nullptr};
   uint32_t* fi[kMaxLevels] = {nullptr};
   int64_t* desc[kMaxLevels] = {nullptr};
   int64_t* doff[kMaxLevels] = {nullptr};
@@ -61,13 +88,13 @@ struct WsPtrs {
 
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
-template <class K>
+template <class KeyT>
 size_t ws_bytes_for(const WsLayout& l, int k) {
   size_t b = 256;  // status word
-  b += 2 * align_up(sizeof(K) * (size_t)l.s1, 256);
+  b += 2 * align_up(sizeof(KeyT) * (size_t)l.s1, 256);
   for (int i = 0; i < kMaxLevels; ++i) {
-    b += align_up(sizeof(K) * (size_t)l.s[i], 256);
-    b += align_up(sizeof(K) * (size_t)l.f[i], 256);
+    b += align_up(sizeof(KeyT) * (size_t)l.s[i], 256);
+    b += align_up(sizeof(KeyT) * (size_t)l.f[i], 256);
     b += align_up(sizeof(uint32_t) * (size_t)l.f[i], 256);
     b += align_up(sizeof(int64_t) * (size_t)l.rows[i] * k, 256);
     b += align_up(sizeof(int64_t) * (size_t)l.rows[i], 256);
@@ -75,9 +102,9 @@ size_t ws_bytes_for(const WsLayout& l, int k) {
   return b + 256;
 }
 
-template <class K>
-WsPtrs<K> ws_carve(const WsLayout& l, int k, void* base) {
-  WsPtrs<K> p;
+template <class KeyT>
+WsPtrs<KeyT> ws_carve(const WsLayout& l, int k, void* base) {
+  WsPtrs<KeyT> p;
   char* c = (char*)align_up((size_t)base, 256);
   auto take = [&](size_t bytes) {
     char* r = c;
@@ -85,11 +112,11 @@ WsPtrs<K> ws_carve(const WsLayout& l, int k, void* base) {
     return r;
   };
   p.err = (int*)take(256);
-  p.s1[0] = (K*)take(sizeof(K) * (size_t)l.s1);
-  p.s1[1] = (K*)take(sizeof(K) * (size_t)l.s1);
+  p.s1[0] = (KeyT*)take(sizeof(KeyT) * (size_t)l.s1);
+  p.s1[1] = (KeyT*)take(sizeof(KeyT) * (size_t)l.s1);
   for (int i = 0; i < kMaxLevels; ++i) {
-    p.s[i] = (K*)take(sizeof(K) * (size_t)l.s[i]);
-    p.fk[i] = (K*)take(sizeof(K) * (size_t)l.f[i]);
+    p.s[i] = (KeyT*)take(sizeof(KeyT) * (size_t)l.s[i]);
+    p.fk[i] = (KeyT*)take(sizeof(KeyT) * (size_t)l.f[i]);
     p.fi[i] = (uint32_t*)take(sizeof(uint32_t) * (size_t)l.f[i]);
     p.desc[i] = (int64_t*)take(sizeof(int64_t) * (size_t)l.rows[i] * k);
     p.doff[i] = (int64_t*)take(sizeof(int64_t) * (size_t)l.rows[i]);
@@ -126,7 +153,7 @@ inline cudaError_t ensure_smem(const void* kern, size_t bytes) {
 //   Cmp    strict weak order on K
 //   Codec  user bits <-> K
 //   STABLE stable base case (key/value sorts, user comparators)
-template <class K, class V, class Cmp, class Codec, bool STABLE, int NT, int ITEMS>
+template <class KeyT, class V, class Cmp, class Codec, bool STABLE, int NT, int ITEMS>
 struct Engine {
   static constexpr int CAP = NT * ITEMS;
   using IdxT = uint32_t;
@@ -142,11 +169,11 @@ struct Engine {
   static void plan_round(WsLayout& l, int level, int64_t n, int64_t L, const Tune& t, bool gather0 = false) {
     const int k = t.k;
     if ((int64_t)k * L <= CAP) return;  // GROUP mode, no scratch
-    const int B = t.sample_b;
-    const int64_t G = CAP / B - k;
+    const int sb = t.sample_b;
+    const int64_t G = CAP / sb - k;
     const int64_t runs = ceil_div(n, L);
-    const int64_t Ls = ceil_div(L, B);
-    const int64_t ns = (runs - 1) * Ls + ceil_div(n - (runs - 1) * L, B);
+    const int64_t Ls = ceil_div(L, sb);
+    const int64_t ns = (runs - 1) * Ls + ceil_div(n - (runs - 1) * L, sb);
     const int64_t groups = ceil_div(n, L * k);
     const int64_t tiles_full = ceil_div((int64_t)k * Ls, G);
     const int64_t rows = groups * (tiles_full + 1);
@@ -179,28 +206,32 @@ struct Engine {
 
   // ---------------- launches ----------------
   template <int MODE, class VV>
-  static cudaError_t launch_tile(const TileArgs<K, VV>& a, int64_t grid, cudaStream_t st) {
+  static cudaError_t launch_tile(const TileArgs<KeyT, VV>& a, int64_t grid, cudaStream_t st, int level = 0) {
     if (grid <= 0) return cudaSuccess;
     constexpr bool kStable = (MODE == MODE_BASE) ? STABLE : false;
-    auto kern = tile_kernel<K, VV, Cmp, Codec, MODE, kStable, NT, ITEMS>;
-    const size_t smem = TileSmemLayout<K, VV, CAP>::bytes;
+    auto kern = tile_kernel<KeyT, VV, Cmp, Codec, MODE, kStable, NT, ITEMS>;
+    const size_t smem = TileSmemLayout<KeyT, VV, CAP>::bytes;
     cudaError_t e = ensure_smem((const void*)kern, smem);
     if (e != cudaSuccess) return e;
     if (grid > 0x7fffffff) return cudaErrorInvalidConfiguration;
+    const int kc = (MODE == MODE_BASE) ? KC_BASE : (level == 0 ? KC_MERGE : KC_SAMPLE_MERGE);
+    hook_before(kc, st);
     kern<<<(unsigned)grid, NT, smem, st>>>(a);
-    return cudaGetLastError();
+    e = cudaGetLastError();
+    hook_after(kc, st);
+    return e;
   }
 
   // One K-way round over runs of length L.  `sample_in` is the block sample of
   // `in` (null: gather it here); `sample_out` receives the block sample of the
   // output runs (null: not needed).
   template <class VV>
-  static cudaError_t round(const WsPtrs<K>& w, int level, const K* in, const VV* vin, K* out, VV* vout, int64_t n,
-                           int64_t L, const Tune& t, const K* sample_in, K* sample_out, int enc, int dec,
+  static cudaError_t round(const WsPtrs<KeyT>& w, int level, const KeyT* in, const VV* vin, KeyT* out, VV* vout, int64_t n,
+                           int64_t L, const Tune& t, const KeyT* sample_in, KeyT* sample_out, int enc, int dec,
                            int gen_index, cudaStream_t st) {
     const int k = t.k;
-    const int B = t.sample_b;
-    TileArgs<K, VV> a{};
+    const int sb = t.sample_b;
+    TileArgs<KeyT, VV> a{};
     a.in = in;
     a.out = out;
     a.vin = vin;
@@ -213,25 +244,28 @@ struct Engine {
     a.gen_index = gen_index;
     a.err = w.err;
     a.sample_out = sample_out;
-    a.sample_b = B;
+    a.sample_b = sb;
     a.out_run_len = L * k;
-    a.sample_run_len = ceil_div(L * k, B);
+    a.sample_run_len = ceil_div(L * k, sb);
     const int64_t groups = ceil_div(n, L * k);
     if ((int64_t)k * L <= CAP) {
-      return launch_tile<MODE_GROUP>(a, groups, st);
+      return launch_tile<MODE_GROUP>(a, groups, st, level);
     }
     if (level + 1 >= kMaxLevels) return cudaErrorInvalidValue;
-    const int64_t G = CAP / B - k;
+    const int64_t G = CAP / sb - k;
     const int64_t runs = ceil_div(n, L);
-    const int64_t Ls = ceil_div(L, B);
-    const int64_t ns = (runs - 1) * Ls + ceil_div(n - (runs - 1) * L, B);
+    const int64_t Ls = ceil_div(L, sb);
+    const int64_t ns = (runs - 1) * Ls + ceil_div(n - (runs - 1) * L, sb);
     cudaError_t e;
-    const K* S = sample_in;
+    const KeyT* S = sample_in;
     if (!S) {
-      K* g = w.s[level + 1];
+      KeyT* g = w.s[level + 1];
       const int64_t slots = runs * Ls;
-      gather_sample_kernel<K, Codec><<<(unsigned)ceil_div(slots, 256), 256, 0, st>>>(in, g, n, L, Ls, B, slots, enc);
-      if ((e = cudaGetLastError()) != cudaSuccess) return e;
+      hook_before(KC_GATHER, st);
+      gather_sample_kernel<KeyT, Codec><<<(unsigned)ceil_div(slots, 256), 256, 0, st>>>(in, g, n, L, Ls, sb, slots, enc);
+      e = cudaGetLastError();
+      hook_after(KC_GATHER, st);
+      if (e != cudaSuccess) return e;
       S = g;
     }
     // 1. merge the block samples of each group, keeping each sample's index
@@ -245,10 +279,13 @@ struct Engine {
     const int64_t rows = groups * (tiles_full + 1);
     {
       const int64_t threads = rows * 32;
-      splitter_kernel<K, Cmp, Codec><<<(unsigned)ceil_div(threads, 256), 256, 0, st>>>(
-          in, w.fk[level + 1], w.fi[level + 1], n, L, k, Ls, B, G, tiles_full, tiles_last, groups, w.desc[level],
+      hook_before(KC_SPLIT, st);
+      splitter_kernel<KeyT, Cmp, Codec><<<(unsigned)ceil_div(threads, 256), 256, 0, st>>>(
+          in, w.fk[level + 1], w.fi[level + 1], n, L, k, Ls, sb, G, tiles_full, tiles_last, groups, w.desc[level],
           w.doff[level], enc);
-      if ((e = cudaGetLastError()) != cudaSuccess) return e;
+      e = cudaGetLastError();
+      hook_after(KC_SPLIT, st);
+      if (e != cudaSuccess) return e;
     }
     // 3. merge the tiles
     a.desc = w.desc[level];
@@ -256,21 +293,21 @@ struct Engine {
     a.tiles_full = tiles_full;
     a.tiles_last = tiles_last;
     a.groups = groups;
-    return launch_tile<MODE_TILE>(a, groups * tiles_full, st);
+    return launch_tile<MODE_TILE>(a, groups * tiles_full, st, level);
   }
 
   // Full sort.  Result in `out` (keys) / `vout` (payload); `in`/`vin` are
   // clobbered.  enc/dec: apply the codec on the first load / last store.
-  static cudaError_t sort(const WsPtrs<K>& w, K* in, V* vin, K* out, V* vout, int64_t n, const Tune& t,
+  static cudaError_t sort(const WsPtrs<KeyT>& w, KeyT* in, V* vin, KeyT* out, V* vout, int64_t n, const Tune& t,
                           cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     const int P = passes_for(n, t.k);
-    K* buf[2] = {in, out};
+    KeyT* buf[2] = {in, out};
     V* vbuf[2] = {vin, vout};
     // base case: P odd -> in place on `in`; P even -> `in` to `out`
     int cur = (P % 2 == 1) ? 0 : 1;
     {
-      TileArgs<K, V> a{};
+      TileArgs<KeyT, V> a{};
       a.in = in;
       a.out = buf[cur];
       a.vin = vin;
@@ -293,7 +330,7 @@ struct Engine {
     int64_t L = CAP;
     for (int p = 0; p < P; ++p) {
       const bool last = (p == P - 1);
-      K* sout = last ? nullptr : w.s1[sbuf ^ 1];
+      KeyT* sout = last ? nullptr : w.s1[sbuf ^ 1];
       cudaError_t e = round<V>(w, 0, buf[cur], vbuf[cur], buf[cur ^ 1], vbuf[cur ^ 1], n, L, t, w.s1[sbuf], sout, 0,
                                last ? 1 : 0, 0, st);
       if (e != cudaSuccess) return e;
@@ -305,14 +342,14 @@ struct Engine {
   }
 
   // One merge round on caller data (the multimergeLevel contract).
-  static cudaError_t merge_level(const WsPtrs<K>& w, const K* in, K* out, int64_t n, int64_t L, const Tune& t,
+  static cudaError_t merge_level(const WsPtrs<KeyT>& w, const KeyT* in, KeyT* out, int64_t n, int64_t L, const Tune& t,
                                  cudaStream_t st) {
     return round<V>(w, 0, in, nullptr, out, nullptr, n, L, t, nullptr, nullptr, 1, 1, 0, st);
   }
 
   // Base case only: every `tile`-key tile sorted (the squareSort contract).
-  static cudaError_t tile_sort(K* data, int64_t n, int64_t tile, cudaStream_t st) {
-    TileArgs<K, V> a{};
+  static cudaError_t tile_sort(KeyT* data, int64_t n, int64_t tile, cudaStream_t st) {
+    TileArgs<KeyT, V> a{};
     a.in = data;
     a.out = data;
     a.n = n;

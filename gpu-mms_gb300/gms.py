@@ -118,6 +118,10 @@ SIGNATURES = {
     "gms_reserve": (_i32, [_i32, _i32, _i64, _vp]),
     "gms_device_status": (_i32, [_vp, ctypes.POINTER(ctypes.c_int)]),
     "gms_release_workspaces": (None, []),
+    "gms_launch_count": (ctypes.c_longlong, []),
+    "gms_timing_enable": (_i32, [_i32]),
+    "gms_timing_collect": (_i32, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong), _i32]),
+    "gms_timing_reset": (_i32, []),
     "gms_rounds": (_i32, [_i32, _i32, _i64]),
     "gms_base_tile": (_i64, [_i32, _i32]),
 }
@@ -249,6 +253,19 @@ def find_partitions(task, size, k, ranks, stream=None):
     _check(lib.gms_find_partitions_i32(task.data_ptr(), size, k, task.numel(), ranks.data_ptr(), ranks.numel(),
                                        out.data_ptr(), _stream_ptr(stream)), "find_partitions")
     return out
+
+
+KERNEL_CLASSES = ["base_tile_sort", "merge_round", "sample_merge", "splitter", "sample_gather", "corank"]
+
+
+def timing_collect():
+    """Per kernel class: (milliseconds, timed launches) since the last reset."""
+    lib = load()
+    n = len(KERNEL_CLASSES)
+    ms = (ctypes.c_double * n)()
+    cnt = (ctypes.c_longlong * n)()
+    _check(lib.gms_timing_collect(ms, cnt, n), "timing_collect")
+    return {name: (ms[i], cnt[i]) for i, name in enumerate(KERNEL_CLASSES)}
 
 
 def device_status(stream=None):

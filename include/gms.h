@@ -156,6 +156,21 @@ void gms_release_workspaces(void);
  * No reference counterpart (the reference reports nothing from its kernels). */
 int gms_device_status(void* stream, int* status_out);
 
+/* ---------------------------------------------------------------------------
+ * Instrumentation (no reference counterpart: the reference times the whole
+ * call with cudaEvents in its driver, src/testMM.cu:170-186).
+ * Kernel classes: 0 base-case tile sort, 1 data merge round, 2 sample merge,
+ * 3 splitter, 4 sample gather, 5 co-rank.
+ * ------------------------------------------------------------------------- */
+/* Total kernels this library has launched in the process. */
+long long gms_launch_count(void);
+/* While on, every launch is bracketed by CUDA events on its own stream. */
+int gms_timing_enable(int on);
+/* Waits for the recorded events and returns, per kernel class (up to
+ * nclasses entries), the accumulated milliseconds and timed launches. */
+int gms_timing_collect(double* ms, long long* launches, int nclasses);
+int gms_timing_reset(void);
+
 /* Number of merge rounds (after the base case) a sort of n keys of the given
  * dtype performs, and the base tile (keys) it uses. */
 int gms_rounds(int dtype, int kv, int64_t n);

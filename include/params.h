@@ -1,0 +1,66 @@
+/*
+ * params.h -- compile-time parameters, GB300 build.
+ *
+ * Keeps the names of the reference's tunables (GPU-MMS src/params.h:18-38) so
+ * code written against the reference still compiles, but every one is guarded
+ * by #ifndef (the reference's unguarded #defines made -D overrides silently
+ * ineffective).  Only GMS_K and GMS_SAMPLE_B feed the GB300 engine; the
+ * reference's K/PL/BLOCKS/PIPELINE/PIVOT_MOVES/THREADS/M/ELTS/W/B describe its
+ * heap merge and are kept for source compatibility only.
+ */
+#ifndef GMS_PARAMS_H_
+#define GMS_PARAMS_H_
+
+/* ---- GB300 engine ---- */
+#ifndef GMS_K
+#define GMS_K 32        /* fan-in of a merge round (2..32)                     */
+#endif
+#ifndef GMS_SAMPLE_B
+#define GMS_SAMPLE_B 32 /* block size of the forecast sample that cuts tiles    */
+#endif
+
+/* ---- reference names (src/params.h:18-38), informational ---- */
+#ifndef BLOCKS
+#define BLOCKS 482
+#endif
+#ifndef K
+#define K 64
+#endif
+#ifndef PL
+#define PL 6
+#endif
+#ifndef PIVOT_MOVES
+#define PIVOT_MOVES 1
+#endif
+#ifndef W
+#define W 32
+#endif
+#ifndef LOGW
+#define LOGW 5
+#endif
+#ifndef B
+#define B 32
+#endif
+#ifndef LOGB
+#define LOGB 5
+#endif
+#ifndef THREADS
+#define THREADS (W * PL)
+#endif
+#ifndef THREADS_BASE_CASE
+#define THREADS_BASE_CASE 32
+#endif
+#ifndef RANGE
+#define RANGE 1024
+#endif
+#ifndef ELTS
+#define ELTS 32
+#endif
+#ifndef M
+#define M 1024
+#endif
+#ifndef FULL_MASK
+#define FULL_MASK 0xFFFFFFFF
+#endif
+
+#endif /* GMS_PARAMS_H_ */
