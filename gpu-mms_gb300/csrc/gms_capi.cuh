@@ -31,7 +31,9 @@ void clear_error();
 // Scratch cache.  `tag` separates independent buffers of one call.
 void* cache_get(int tag, size_t bytes, cudaStream_t st, int* status);
 
-inline gms::Tune default_tune() { return gms::Tune{}; }
+// Process-wide tuning (gms_set_tune); defaults are gms::Tune{}.
+gms::Tune current_tune();
+inline gms::Tune default_tune() { return current_tune(); }
 
 // Runs a full sort of one dtype with the scratch cache.
 template <class Eng, class K, class V>

@@ -74,6 +74,16 @@ void* cache_get(int tag, size_t bytes, cudaStream_t st, int* status) {
   return p;
 }
 
+// ---- tuning ----
+namespace {
+std::mutex g_tune_mu;
+gms::Tune g_tune;
+}  // namespace
+gms::Tune current_tune() {
+  std::lock_guard<std::mutex> g(g_tune_mu);
+  return g_tune;
+}
+
 // ---- launch counting and live kernel timing ----
 namespace {
 struct TimedLaunch {
@@ -152,6 +162,26 @@ void gms_release_workspaces(void) {
     cudaSetDevice(cur);
   }
   g_slots.clear();
+}
+
+int gms_set_tune(int k, int sample_b, int bulk_copy) {
+  clear_error();
+  if (k < 2 || k > 32) return set_error(GMS_ERR_INVALID, "k must be in [2, 32]");
+  if (sample_b < 1 || (int64_t)kNT * kItems / sample_b - k < 1)
+    return set_error(GMS_ERR_INVALID, "sample_b leaves no room for a tile (need CAP/sample_b > k)");
+  std::lock_guard<std::mutex> g(g_tune_mu);
+  g_tune.k = k;
+  g_tune.sample_b = sample_b;
+  g_tune.bulk_copy = bulk_copy ? 1 : 0;
+  return GMS_OK;
+}
+
+int gms_get_tune(int* k, int* sample_b, int* bulk_copy) {
+  std::lock_guard<std::mutex> g(g_tune_mu);
+  if (k) *k = g_tune.k;
+  if (sample_b) *sample_b = g_tune.sample_b;
+  if (bulk_copy) *bulk_copy = g_tune.bulk_copy;
+  return GMS_OK;
 }
 
 long long gms_launch_count(void) {

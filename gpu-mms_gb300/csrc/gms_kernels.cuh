@@ -16,6 +16,7 @@
 #pragma once
 
 #include "gms_device.cuh"
+#include "gms_tma.cuh"
 
 namespace gms {
 
@@ -50,7 +51,7 @@ struct TileArgs {
 };
 
 // Bits of the device status word.
-enum DeviceStatus : int { DEV_TILE_OVERFLOW = 1, DEV_BAD_SEGMENT = 2 };
+enum DeviceStatus : int { DEV_TILE_OVERFLOW = 1, DEV_BAD_SEGMENT = 2, DEV_COPY_TIMEOUT = 4 };
 
 template <class KeyT, class V, int CAP>
 struct TileSmemLayout {
@@ -73,6 +74,16 @@ template <class Codec, class KeyT>
 __device__ __forceinline__ KeyT maybe_dec(KeyT x, int on) {
   return on ? Codec::dec(x) : x;
 }
+
+// Comparator on raw user bits that encodes both sides first (when `on`).
+template <class Cmp, class Codec>
+struct EncCmp {
+  int on;
+  template <class KeyT>
+  __device__ __forceinline__ bool operator()(const KeyT& x, const KeyT& y) const {
+    return Cmp()(maybe_enc<Codec>(x, on), maybe_enc<Codec>(y, on));
+  }
+};
 
 // ---------------------------------------------------------------------------
 // The tile kernel.
@@ -297,6 +308,360 @@ __global__ void __launch_bounds__(NT) tile_kernel(TileArgs<KeyT, V> a) {
     for (int64_t p = first + (int64_t)tid * a.sample_b; p < cnt; p += (int64_t)NT * a.sample_b) {
       a.sample_out[run_index * a.sample_run_len + (rel0 + p) / a.sample_b] = sk[p];
     }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Persistent K-way merge of forecast tiles with bulk-copy staging.
+//
+// Each CTA walks tiles blockIdx.x, blockIdx.x + gridDim.x, ...  For each tile,
+// warp 0 places the K run segments in the staging buffer (16-byte-aligned
+// regions) and issues one cp.async.bulk per segment, completing on an
+// mbarrier.  The first merge level reads the staged segments directly and
+// writes the merged pairs to the merge buffer; the staging buffer is then free
+// and warp 0 immediately issues the NEXT tile's copies, which land while the
+// remaining ceil(log2 K)-1 levels and the store of the current tile run.
+template <class KeyT, class V, int CAP>
+struct MergeSmemLayout {
+  static constexpr bool kHasVal = HasVal<V>::value;
+  static constexpr int kMaxK = 32;
+  static constexpr size_t round16(size_t x) { return (x + 15) / 16 * 16; }
+  // every segment region may add up to 30 bytes of alignment slack
+  static constexpr size_t stage_k_bytes = round16(sizeof(KeyT) * (CAP + 1) + 32 * kMaxK + 16);
+  static constexpr size_t stage_v_bytes = kHasVal ? round16(sizeof(V) * (CAP + 1) + 32 * kMaxK + 16) : 0;
+  static constexpr size_t mk_bytes = round16(sizeof(KeyT) * (CAP + 1));
+  static constexpr size_t mv_bytes = kHasVal ? round16(sizeof(V) * (CAP + 1)) : 0;
+  static constexpr size_t off_stage_v = stage_k_bytes;
+  static constexpr size_t off_mk = off_stage_v + stage_v_bytes;
+  static constexpr size_t off_mv = off_mk + mk_bytes;
+  static constexpr size_t off_desc = off_mv + mv_bytes;
+  // descriptors, double-buffered: cpre[2][33] int, sbk[2][32] int, sbv[2][32] int,
+  // gsrc[2][32] int64, meta[2][4] int64, bar (8 bytes)
+  static constexpr size_t desc_bytes = 2 * (33 + 32 + 32) * 4 + 4 + 2 * 32 * 8 + 2 * 4 * 8 + 16;
+  static constexpr size_t bytes = off_desc + desc_bytes;
+};
+
+template <class KeyT, class V, class Cmp, class Codec, int NT, int ITEMS>
+__global__ void __launch_bounds__(NT, 2) merge_tiles_kernel(TileArgs<KeyT, V> a, int64_t total_tiles) {
+  constexpr int CAP = NT * ITEMS;
+  constexpr bool kHasVal = HasVal<V>::value;
+  using Lay = MergeSmemLayout<KeyT, V, CAP>;
+  constexpr int kMaxK = Lay::kMaxK;
+  extern __shared__ __align__(16) unsigned char smem[];
+  unsigned char* stage_k = smem;
+  unsigned char* stage_v = smem + Lay::off_stage_v;
+  KeyT* mk = reinterpret_cast<KeyT*>(smem + Lay::off_mk);
+  V* mv = reinterpret_cast<V*>(smem + Lay::off_mv);
+  int* cpre_all = reinterpret_cast<int*>(smem + Lay::off_desc);  // [2][33]
+  int* sbk_all = cpre_all + 2 * 33;                                // [2][32]
+  int* sbv_all = sbk_all + 2 * 32;                                 // [2][32]
+  int64_t* gsrc_all = reinterpret_cast<int64_t*>(smem + Lay::off_desc + ((2 * 97 * 4 + 4 + 7) / 8) * 8);
+  int64_t* meta_all = gsrc_all + 2 * 32;  // [2][4]: out_base, run_base, run_index, cnt|bad
+  uint64_t* bar = reinterpret_cast<uint64_t*>(meta_all + 2 * 4);
+  const Cmp cmp;
+  const int tid = threadIdx.x;
+  const int lane = tid & 31;
+  const int nk = a.k;
+  const uint64_t arr_k_lo = reinterpret_cast<uint64_t>(a.in);
+  const uint64_t arr_k_hi = arr_k_lo + (uint64_t)a.n * sizeof(KeyT);
+  uint64_t arr_v_lo = 0, arr_v_hi = 0;
+  if constexpr (kHasVal) {
+    if (!a.gen_index) {
+      arr_v_lo = reinterpret_cast<uint64_t>(a.vin);
+      arr_v_hi = arr_v_lo + (uint64_t)a.n * sizeof(V);
+    }
+  }
+
+  auto tile_valid = [&](int64_t tau) -> bool {
+    if (tau >= total_tiles) return false;
+    const int64_t g = tau / a.tiles_full;
+    const int64_t j = tau - g * a.tiles_full;
+    const int64_t jg = (g == a.groups - 1) ? a.tiles_last : a.tiles_full;
+    return j < jg;
+  };
+  auto next_tile = [&](int64_t tau) -> int64_t {
+    tau += gridDim.x;
+    while (tau < total_tiles && !tile_valid(tau)) tau += gridDim.x;
+    return tau;
+  };
+
+  // Warp 0: place and issue the copies of tile `tau` into descriptor slot d.
+  auto issue = [&](int64_t tau, int d) {
+    const int64_t g = tau / a.tiles_full;
+    const int64_t j = tau - g * a.tiles_full;
+    const int64_t gbase = g * a.L * a.k;
+    const int64_t row = g * (a.tiles_full + 1) + j;
+    const int64_t ng = min64(a.L * a.k, a.n - gbase);
+    int len = 0;
+    int64_t gs = 0;
+    bool bad = false;
+    if (lane < nk) {
+      const int64_t lo = a.desc[row * nk + lane];
+      const int64_t hi = a.desc[(row + 1) * nk + lane];
+      const int64_t rl = min64(a.L, ng - min64((int64_t)lane * a.L, ng));
+      bad = !((lo >= 0) && (hi >= lo) && (hi <= rl) && (hi - lo <= CAP));
+      len = bad ? 0 : (int)(hi - lo);
+      gs = gbase + (int64_t)lane * a.L + (bad ? 0 : lo);
+    }
+    // compact prefix of lengths
+    int incl = len;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    const bool any_bad = __any_sync(0xffffffffu, bad) || total > CAP;
+    int* cpre = cpre_all + d * 33;
+    if (lane < nk) cpre[lane + 1] = incl;
+    if (lane == 0) cpre[0] = 0;
+    // key regions
+    const uint64_t A = arr_k_lo + (uint64_t)gs * sizeof(KeyT);
+    const uint64_t E = A + (uint64_t)len * sizeof(KeyT);
+    const SegCopy ck = seg_copy(A, E, arr_k_lo, arr_k_hi);
+    const uint32_t reg_k = (uint32_t)(ck.e16 - ck.a16);
+    uint32_t off_k = reg_k;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, off_k, o);
+      if (lane >= o) off_k += y;
+    }
+    off_k -= reg_k;  // exclusive
+    uint32_t bulk = (!any_bad && ck.be > ck.bs) ? (uint32_t)(ck.be - ck.bs) : 0u;
+    SegCopy cv{};
+    uint32_t off_v = 0;
+    if constexpr (kHasVal) {
+      if (!a.gen_index) {
+        const uint64_t Av = arr_v_lo + (uint64_t)gs * sizeof(V);
+        const uint64_t Ev = Av + (uint64_t)len * sizeof(V);
+        cv = seg_copy(Av, Ev, arr_v_lo, arr_v_hi);
+        const uint32_t reg_v = (uint32_t)(cv.e16 - cv.a16);
+        off_v = reg_v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t y = __shfl_up_sync(0xffffffffu, off_v, o);
+          if (lane >= o) off_v += y;
+        }
+        off_v -= reg_v;
+        if (!any_bad && cv.be > cv.bs) bulk += (uint32_t)(cv.be - cv.bs);
+      }
+    }
+    uint32_t tx = bulk;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) tx += __shfl_xor_sync(0xffffffffu, tx, o);
+    if (lane < nk) {
+      sbk_all[d * 32 + lane] = (int)((off_k + (uint32_t)(A - ck.a16)) / sizeof(KeyT));
+      gsrc_all[d * 32 + lane] = gs;
+      if constexpr (kHasVal) {
+        if (!a.gen_index) {
+          sbv_all[d * 32 + lane] = (int)((off_v + (uint32_t)((arr_v_lo + (uint64_t)gs * sizeof(V)) - cv.a16)) / sizeof(V));
+        }
+      }
+    }
+    if (lane == 0) {
+      int64_t* meta = meta_all + d * 4;
+      meta[0] = gbase + a.doff[row];
+      meta[1] = gbase;
+      meta[2] = g;
+      meta[3] = any_bad ? -1 : total;
+      if (any_bad && a.err) atomicOr(a.err, DEV_BAD_SEGMENT);
+    }
+    // staging buffers were read by the generic proxy; order before bulk writes
+    fence_proxy_async_smem();
+    if (lane == 0) mbar_arrive_expect_tx(bar, tx);
+    __syncwarp();
+    if (!any_bad && lane < nk && len > 0) {
+      unsigned char* dstk = stage_k + off_k;
+      if (ck.be > ck.bs) {
+        bulk_g2s(dstk + (ck.bs - ck.a16), reinterpret_cast<const void*>(ck.bs), (uint32_t)(ck.be - ck.bs), bar);
+      }
+      // plain loads for the bytes outside the array's aligned interior
+      const KeyT* src = a.in + gs;
+      KeyT* dst = reinterpret_cast<KeyT*>(dstk + (A - ck.a16));
+      for (int i = 0; i < len; ++i) {
+        const uint64_t addr = A + (uint64_t)i * sizeof(KeyT);
+        const bool in_bulk = (ck.be > ck.bs) && addr >= ck.bs && addr < ck.be;
+        if (!in_bulk) dst[i] = src[i];
+        if (ck.be > ck.bs && addr >= ck.bs && addr < ck.be) {
+          // skip the bulk interior in one step
+          const int64_t skip = (int64_t)((ck.be - addr) / sizeof(KeyT)) - 1;
+          i += (int)skip;
+        }
+      }
+      if constexpr (kHasVal) {
+        if (!a.gen_index) {
+          unsigned char* dstv = stage_v + off_v;
+          const uint64_t Av = arr_v_lo + (uint64_t)gs * sizeof(V);
+          if (cv.be > cv.bs) {
+            bulk_g2s(dstv + (cv.bs - cv.a16), reinterpret_cast<const void*>(cv.bs), (uint32_t)(cv.be - cv.bs), bar);
+          }
+          const V* vsrc = a.vin + gs;
+          V* vdst = reinterpret_cast<V*>(dstv + (Av - cv.a16));
+          for (int i = 0; i < len; ++i) {
+            const uint64_t addr = Av + (uint64_t)i * sizeof(V);
+            const bool in_bulk = (cv.be > cv.bs) && addr >= cv.bs && addr < cv.be;
+            if (!in_bulk) vdst[i] = vsrc[i];
+            if (in_bulk) {
+              const int64_t skip = (int64_t)((cv.be - addr) / sizeof(V)) - 1;
+              i += (int)skip;
+            }
+          }
+        }
+      }
+    }
+  };
+
+  if (tid == 0) mbar_init(bar, 1);
+  fence_mbar_init();
+  __syncthreads();
+
+  int64_t tau = blockIdx.x;
+  while (tau < total_tiles && !tile_valid(tau)) tau += gridDim.x;
+  if (tau >= total_tiles) return;
+  if (tid < 32) issue(tau, 0);
+  uint32_t phase = 0;
+  int d = 0;
+  constexpr uint32_t kSpinLimit = 1u << 26;
+
+  while (tau < total_tiles) {
+    // ---- wait for this tile's staged segments ----
+    if (!mbar_wait_bounded(bar, phase, kSpinLimit)) {
+      if (tid == 0 && a.err) atomicOr(a.err, DEV_COPY_TIMEOUT);
+      mbar_wait_bounded(bar, phase, kSpinLimit);  // let copies in flight land
+      return;
+    }
+    phase ^= 1u;
+    __syncthreads();  // plain-loaded bytes from warp 0 are visible
+    const int* cpre = cpre_all + d * 33;
+    const int64_t* meta = meta_all + d * 4;
+    const int cnt = (int)meta[3];
+    const int64_t out_base = meta[0];
+    const int64_t run_base = meta[1];
+    const int64_t run_index = meta[2];
+    const int64_t next = next_tile(tau);
+    if (cnt < 0) {
+      // rejected tile (never expected): skip it, keep the pipeline going
+      __syncthreads();
+      if (next < total_tiles && tid < 32) issue(next, d ^ 1);
+      tau = next;
+      d ^= 1;
+      continue;
+    }
+    const int s = tid * ITEMS;
+    const int e = min(s + ITEMS, cnt);
+    KeyT ok[ITEMS];
+    V ov[ITEMS];
+    // ---- level 1: staged segment pairs -> merge buffer ----
+    if (s < cnt) {
+      const int* sbk = sbk_all + d * 32;
+      const int* sbv = sbv_all + d * 32;
+      const int64_t* gsrc = gsrc_all + d * 32;
+      const KeyT* sk = reinterpret_cast<const KeyT*>(stage_k);
+      const V* sv = reinterpret_cast<const V*>(stage_v);
+      const int npairs = (nk + 1) / 2;
+      int lo = 0, hi = npairs - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (cpre[2 * mid] <= s) lo = mid; else hi = mid - 1;
+      }
+      int p = lo;
+      auto setup = [&](int pp, const KeyT*& A, const KeyT*& Bp, int& na, int& nb, int& base) {
+        const int ka = 2 * pp;
+        const int kb = min(2 * pp + 1, nk);
+        base = cpre[ka];
+        na = cpre[ka + 1] - cpre[ka];
+        nb = (kb < nk) ? cpre[kb + 1] - cpre[kb] : 0;
+        A = sk + sbk[ka];
+        Bp = (kb < nk) ? sk + sbk[kb] : A + na;
+      };
+      const KeyT* A;
+      const KeyT* Bq;
+      int na, nb, base;
+      setup(p, A, Bq, na, nb, base);
+      const int enc = a.enc_on_load;
+      const EncCmp<Cmp, Codec> ecmp{enc};
+      const int diag = s - base;
+      int ia = merge_path(A, na, Bq, nb, diag, ecmp);
+      int ib = diag - ia;
+      KeyT ka = maybe_enc<Codec>(A[ia], enc);
+      KeyT kb = maybe_enc<Codec>(Bq[ib], enc);
+#pragma unroll
+      for (int i = 0; i < ITEMS; ++i) {
+        if (s + i < e) {
+          if (ia >= na && ib >= nb) {
+            const int q = s + i;
+            int l2 = p + 1, h2 = npairs - 1;
+            while (l2 < h2) {
+              const int mid = (l2 + h2 + 1) >> 1;
+              if (cpre[2 * mid] <= q) l2 = mid; else h2 = mid - 1;
+            }
+            p = l2 < npairs - 1 ? l2 : npairs - 1;
+            setup(p, A, Bq, na, nb, base);
+            ia = 0;
+            ib = 0;
+            ka = maybe_enc<Codec>(A[0], enc);
+            kb = maybe_enc<Codec>(Bq[0], enc);
+          }
+          const bool ta = (ib >= nb) || ((ia < na) && !cmp(kb, ka));
+          ok[i] = ta ? ka : kb;
+          if constexpr (kHasVal) {
+            const int seg = ta ? 2 * p : 2 * p + 1;
+            const int off = ta ? ia : ib;
+            if (a.gen_index) {
+              ov[i] = (V)(gsrc[seg] + off);
+            } else {
+              ov[i] = sv[sbv[seg] + off];
+            }
+          }
+          if (ta) {
+            ++ia;
+            ka = maybe_enc<Codec>(A[ia], enc);
+          } else {
+            ++ib;
+            kb = maybe_enc<Codec>(Bq[ib], enc);
+          }
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < ITEMS; ++i) {
+        if (s + i < e) {
+          mk[s + i] = ok[i];
+          if constexpr (kHasVal) mv[s + i] = ov[i];
+        }
+      }
+    }
+    __syncthreads();  // merge buffer complete; staging buffer free
+    if (next < total_tiles && tid < 32) issue(next, d ^ 1);
+    // ---- remaining levels inside the merge buffer ----
+    for (int span = 4; span < 2 * nk; span *= 2) {
+      if (s < cnt) merge_level_var<ITEMS>(mk, mv, cpre, nk, span, s, e, ok, ov, cmp);
+      __syncthreads();
+      if (s < cnt) {
+#pragma unroll
+        for (int i = 0; i < ITEMS; ++i) {
+          if (s + i < e) {
+            mk[s + i] = ok[i];
+            if constexpr (kHasVal) mv[s + i] = ov[i];
+          }
+        }
+      }
+      __syncthreads();
+    }
+    // ---- coalesced store (+ block sample for the next round) ----
+    for (int q = tid; q < cnt; q += NT) {
+      a.out[out_base + q] = maybe_dec<Codec>(mk[q], a.dec_on_store);
+      if constexpr (kHasVal) a.vout[out_base + q] = mv[q];
+    }
+    if (a.sample_out) {
+      const int64_t rel0 = out_base - run_base;
+      const int64_t first = (a.sample_b - rel0 % a.sample_b) % a.sample_b;
+      for (int64_t q = first + (int64_t)tid * a.sample_b; q < cnt; q += (int64_t)NT * a.sample_b) {
+        a.sample_out[run_index * a.sample_run_len + (rel0 + q) / a.sample_b] = mk[q];
+      }
+    }
+    __syncthreads();  // merge buffer free for the next tile
+    tau = next;
+    d ^= 1;
   }
 }
 

@@ -64,6 +64,7 @@ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 struct Tune {
   int k = 32;         // fan-in per round (<= 32)
   int sample_b = 32;  // block size of the forecast sample
+  int bulk_copy = 1;  // 1: persistent merge with bulk-copy staging; 0: one CTA per tile, plain loads
 };
 
 // Scratch layout, computed by a dry run of the same recursion as the real run.
@@ -122,6 +123,34 @@ WsPtrs<KeyT> ws_carve(const WsLayout& l, int k, void* base) {
     p.doff[i] = (int64_t*)take(sizeof(int64_t) * (size_t)l.rows[i]);
   }
   return p;
+}
+
+// Resident CTAs per SM x SM count for a persistent kernel (cached per kernel).
+inline int persistent_grid(const void* kern, int threads, size_t smem, cudaError_t* err) {
+  static std::mutex mu;
+  static const void* keys[64];
+  static int vals[64];
+  static int nk = 0;
+  int dev = 0;
+  *err = cudaGetDevice(&dev);
+  if (*err != cudaSuccess) return 0;
+  std::lock_guard<std::mutex> g(mu);
+  for (int i = 0; i < nk; ++i) {
+    if (keys[i] == kern) return vals[i];
+  }
+  int sms = 0, per = 0;
+  *err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (*err != cudaSuccess) return 0;
+  *err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, threads, smem);
+  if (*err != cudaSuccess) return 0;
+  if (per < 1) per = 1;
+  const int v = sms * per;
+  if (nk < 64) {
+    keys[nk] = kern;
+    vals[nk] = v;
+    ++nk;
+  }
+  return v;
 }
 
 // Per-kernel, per-device opt-in to large dynamic shared memory.
@@ -222,6 +251,26 @@ struct Engine {
     return e;
   }
 
+  // Persistent bulk-copy merge of the forecast tiles of one round.
+  template <class VV>
+  static cudaError_t launch_merge_tiles(const TileArgs<KeyT, VV>& a, int64_t total_tiles, cudaStream_t st,
+                                        int level) {
+    if (total_tiles <= 0) return cudaSuccess;
+    auto kern = merge_tiles_kernel<KeyT, VV, Cmp, Codec, NT, ITEMS>;
+    const size_t smem = MergeSmemLayout<KeyT, VV, CAP>::bytes;
+    cudaError_t e = ensure_smem((const void*)kern, smem);
+    if (e != cudaSuccess) return e;
+    const int pg = persistent_grid((const void*)kern, NT, smem, &e);
+    if (e != cudaSuccess) return e;
+    const int64_t grid = total_tiles < pg ? total_tiles : pg;
+    const int kc = level == 0 ? KC_MERGE : KC_SAMPLE_MERGE;
+    hook_before(kc, st);
+    kern<<<(unsigned)grid, NT, smem, st>>>(a, total_tiles);
+    e = cudaGetLastError();
+    hook_after(kc, st);
+    return e;
+  }
+
   // One K-way round over runs of length L.  `sample_in` is the block sample of
   // `in` (null: gather it here); `sample_out` receives the block sample of the
   // output runs (null: not needed).
@@ -293,6 +342,7 @@ struct Engine {
     a.tiles_full = tiles_full;
     a.tiles_last = tiles_last;
     a.groups = groups;
+    if (t.bulk_copy) return launch_merge_tiles(a, groups * tiles_full, st, level);
     return launch_tile<MODE_TILE>(a, groups * tiles_full, st, level);
   }
 

@@ -119,6 +119,8 @@ SIGNATURES = {
     "gms_device_status": (_i32, [_vp, ctypes.POINTER(ctypes.c_int)]),
     "gms_release_workspaces": (None, []),
     "gms_launch_count": (ctypes.c_longlong, []),
+    "gms_set_tune": (_i32, [_i32, _i32, _i32]),
+    "gms_get_tune": (_i32, [ctypes.POINTER(ctypes.c_int)] * 3),
     "gms_timing_enable": (_i32, [_i32]),
     "gms_timing_collect": (_i32, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong), _i32]),
     "gms_timing_reset": (_i32, []),

@@ -171,6 +171,20 @@ int gms_timing_enable(int on);
 int gms_timing_collect(double* ms, long long* launches, int nclasses);
 int gms_timing_reset(void);
 
+/* ---------------------------------------------------------------------------
+ * Tuning, process-wide, applied to calls that start afterwards.
+ * Replaces the reference's compile-time constants K (fan-in) and PIPELINE /
+ * BLOCKS (src/params.h:18-20), which its sweep scripts tried to override
+ * (scripts/findK.sh, scripts/blocksThreads.sh).
+ *   k          fan-in of a merge round, 2..32 (default 32)
+ *   sample_b   block size of the forecast sample that cuts tiles (default 32;
+ *              needs max_tile/sample_b > k)
+ *   bulk_copy  1: persistent merge kernel staging segments with cp.async.bulk
+ *              (default); 0: one CTA per tile with plain loads
+ * ------------------------------------------------------------------------- */
+int gms_set_tune(int k, int sample_b, int bulk_copy);
+int gms_get_tune(int* k, int* sample_b, int* bulk_copy);
+
 /* Number of merge rounds (after the base case) a sort of n keys of the given
  * dtype performs, and the base tile (keys) it uses. */
 int gms_rounds(int dtype, int kv, int64_t n);

@@ -79,7 +79,9 @@ T* run(T* input, T* output, int N) {
     return nullptr;
   }
   if (N == 0) return output;
-  const gms::Tune t{GMS_K, GMS_SAMPLE_B};
+  gms::Tune t;
+  t.k = GMS_K;
+  t.sample_b = GMS_SAMPLE_B;
   const gms::WsLayout l = Eng::plan((int64_t)N, t);
   cudaError_t e = cudaSuccess;
   void* ws = scratch(gms::ws_bytes_for<T>(l, t.k), &e);

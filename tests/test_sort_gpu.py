@@ -239,3 +239,40 @@ def test_invalid_arguments(gms):
     assert lib.gms_tile_sort_i32(t.data_ptr(), 16, 8705, stream()) == 1
     assert b"n" in lib.gms_last_error() or lib.gms_last_error() != b""
     assert lib.gms_sort_i32(t.data_ptr(), t.data_ptr(), 0, 0, stream()) == 0
+
+
+# ---------------------------------------------------------------------------
+# Tuning: other fan-ins, sample block sizes and both merge paths (bulk-copy
+# persistent merge and one-CTA-per-tile plain loads) must give the same bits.
+TUNES = [(32, 32, 0), (2, 32, 1), (3, 16, 1), (7, 64, 1), (16, 8, 1), (32, 128, 1), (5, 100, 0), (32, 17, 1)]
+
+
+@pytest.fixture
+def tuned(gms):
+    lib = gms.load()
+    yield lib
+    assert lib.gms_set_tune(32, 32, 1) == 0
+
+
+@pytest.mark.parametrize("k,b,bulk", TUNES)
+def test_tune_variants(gms, oracle, tuned, k, b, bulk):
+    lib = tuned
+    assert lib.gms_set_tune(k, b, bulk) == 0
+    for n, dist in [(8705, 6), (300001, 0), (1_234_567, 4), (2_000_003, 1), (1_500_001, 3)]:
+        a = oracle.gen_i32(n, dist, 7 * k + b)
+        assert_same(gpu_sort(gms, a), oracle.sort(a), f"k={k} b={b} bulk={bulk} n={n} dist={dist}")
+    k64 = oracle.gen_u64(700001, k)
+    v = np.arange(k64.size, dtype=np.int32)
+    k64[::2] = k64[1]
+    gk, gv = gpu_sort_kv(gms, k64, v)
+    ok_, ov_ = oracle.sort_kv(k64, v)
+    assert_same(gk, ok_, "kv keys")
+    assert_same(gv, ov_, "kv payload")
+
+
+def test_tune_rejects_bad_values(gms, tuned):
+    lib = tuned
+    assert lib.gms_set_tune(1, 32, 1) == 1
+    assert lib.gms_set_tune(33, 32, 1) == 1
+    assert lib.gms_set_tune(32, 0, 1) == 1
+    assert lib.gms_set_tune(32, 300, 1) == 1  # 8704/300 - 32 < 1
