@@ -167,26 +167,65 @@ __device__ __forceinline__ void transposition_sort(KeyT (&r)[N], V (&v)[N], Cmp 
 
 // ---------------------------------------------------------------------------
 // Merge path: number of elements of `a` among the first `diag` outputs of the
-// stable merge of a and b (a wins ties).
+// stable merge of a and b (a wins ties).  Lower-bound search whose steps are
+// branch-free (selects), so lanes of a warp never diverge inside a step.
 template <class KeyT, class Cmp>
 __device__ __forceinline__ int merge_path(const KeyT* a, int na, const KeyT* b, int nb, int diag, Cmp cmp) {
   int lo = diag - nb > 0 ? diag - nb : 0;
-  int hi = diag < na ? diag : na;
-  while (lo < hi) {
-    const int mid = (lo + hi) >> 1;
-    if (!cmp(b[diag - 1 - mid], a[mid])) {
-      lo = mid + 1;
-    } else {
-      hi = mid;
-    }
+  int len = (diag < na ? diag : na) - lo;
+  while (len > 0) {
+    const int half = len >> 1;
+    const int mid = lo + half;
+    const bool go = !cmp(b[diag - 1 - mid], a[mid]);
+    lo = go ? mid + 1 : lo;
+    len = go ? len - half - 1 : half;
   }
   return lo;
 }
 
+// Cursor of a stable two-way merge over shared memory.  A = [xa, ea),
+// B = [xb, eb) (absolute indices in one buffer); ka/kb hold the heads.  step()
+// emits the smaller head (A wins ties) and advances that side with a single
+// unconditional shared-memory load at index max+1 of the consumed side, which
+// is always inside the buffer (buffers carry one slack element).  No branches.
+template <class KeyT>
+struct MergeCursor {
+  int xa, ea, xb, eb;
+  KeyT ka, kb;
+
+  template <class Cmp>
+  __device__ __forceinline__ void init(const KeyT* sk, int a0, int a1, int b0, int b1, Cmp) {
+    xa = a0;
+    ea = a1;
+    xb = b0;
+    eb = b1;
+    ka = sk[a0];
+    kb = sk[b0];
+  }
+
+  // Returns the emitted key; `src` receives its index, `took_a` its side.
+  template <class Cmp>
+  __device__ __forceinline__ KeyT step(const KeyT* sk, Cmp cmp, int& src, bool& took_a) {
+    const bool ta = (xb >= eb) || ((xa < ea) && !cmp(kb, ka));
+    const KeyT o = ta ? ka : kb;
+    const int cur = ta ? xa : xb;
+    const KeyT nv = sk[cur + 1];
+    xa = ta ? cur + 1 : xa;
+    xb = ta ? xb : cur + 1;
+    ka = ta ? nv : ka;
+    kb = ta ? kb : nv;
+    src = cur;
+    took_a = ta;
+    return o;
+  }
+
+  __device__ __forceinline__ bool exhausted() const { return xa + xb == ea + eb; }
+};
+
 // One level of pairwise merging over runs of equal length `rl` inside a
-// shared-memory tile of `cap` keys (cap a multiple of 2*rl or the tail run
-// shorter).  Thread `t` produces outputs [t*ITEMS, t*ITEMS + ITEMS) into
-// registers.  ITEMS divides rl, so a thread never straddles two pairs.
+// shared-memory tile of `cap` keys.  Thread `t` produces outputs
+// [t*ITEMS, t*ITEMS + ITEMS) into registers.  ITEMS divides rl, so a thread
+// never straddles two pairs.
 template <int ITEMS, class KeyT, class V, class Cmp>
 __device__ __forceinline__ void merge_level_regular(const KeyT* sk, const V* sv, int cap, int rl, int s,
                                                     KeyT (&ok)[ITEMS], V (&ov)[ITEMS], Cmp cmp) {
@@ -195,89 +234,64 @@ __device__ __forceinline__ void merge_level_regular(const KeyT* sk, const V* sv,
   const int pe = min(ps + 2 * rl, cap);
   const int diag = s - ps;
   const int ia = merge_path(sk + ps, pm - ps, sk + pm, pe - pm, diag, cmp);
-  int xa = ps + ia;
-  int xb = pm + (diag - ia);
-  KeyT ka = sk[xa];
-  KeyT kb = sk[xb];
+  MergeCursor<KeyT> c;
+  c.init(sk, ps + ia, pm, pm + (diag - ia), pe, cmp);
 #pragma unroll
   for (int i = 0; i < ITEMS; ++i) {
-    const bool ta = (xb >= pe) || ((xa < pm) && !cmp(kb, ka));
-    ok[i] = ta ? ka : kb;
-    if constexpr (HasVal<V>::value) ov[i] = sv[ta ? xa : xb];
-    if (ta) {
-      ++xa;
-      ka = sk[xa];
-    } else {
-      ++xb;
-      kb = sk[xb];
-    }
+    int src;
+    bool ta;
+    ok[i] = c.step(sk, cmp, src, ta);
+    if constexpr (HasVal<V>::value) ov[i] = sv[src];
   }
 }
 
-// One level of pairwise merging over K variable-length runs whose boundaries
-// are pre[0..K] (pre[K] = total).  At level `span` (2, 4, 8, ...) the runs
+// Locates the pair of level `span` that holds output position q: the largest
+// pair index whose start pre[p*span] is <= q.
+__device__ __forceinline__ int find_pair(const int* pre, int npairs, int span, int q, int lo = 0) {
+  int hi = npairs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    lo = (pre[mid * span] <= q) ? mid : lo;
+    hi = (pre[mid * span] <= q) ? hi : mid - 1;
+  }
+  return lo;
+}
+
+// One level of pairwise merging over nk variable-length runs whose boundaries
+// are pre[0..nk] (pre[nk] = total).  At level `span` (2, 4, 8, ...) the runs
 // [pre[p*span], pre[p*span+span/2]) and [pre[p*span+span/2], pre[p*span+span])
-// are merged.  Runs may be empty; a thread whose ITEMS outputs straddle the end
-// of one pair continues with the next non-empty pair.
+// are merged.  Runs may be empty.  A thread whose outputs reach the end of its
+// pair continues with the next non-empty pair (rare; a uniform branch).  All
+// ITEMS steps run; outputs past the tile end are garbage the caller does not
+// write back.
 template <int ITEMS, class KeyT, class V, class Cmp>
 __device__ __forceinline__ void merge_level_var(const KeyT* sk, const V* sv, const int* pre, int nk, int span,
                                                 int s, int e, KeyT (&ok)[ITEMS], V (&ov)[ITEMS], Cmp cmp) {
+  (void)e;
   const int npairs = (nk + span - 1) / span;
-  // largest pair index whose start is <= s
-  int lo = 0, hi = npairs - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (pre[mid * span] <= s) {
-      lo = mid;
-    } else {
-      hi = mid - 1;
-    }
-  }
-  int p = lo;
+  int p = find_pair(pre, npairs, span, s);
   int ps = pre[p * span];
   int pm = pre[min(p * span + span / 2, nk)];
   int pe = pre[min(p * span + span, nk)];
   const int diag = s - ps;
   const int ia = merge_path(sk + ps, pm - ps, sk + pm, pe - pm, diag, cmp);
-  int xa = ps + ia;
-  int xb = pm + (diag - ia);
-  KeyT ka = sk[xa];
-  KeyT kb = sk[xb];
+  MergeCursor<KeyT> c;
+  c.init(sk, ps + ia, pm, pm + (diag - ia), pe, cmp);
 #pragma unroll
   for (int i = 0; i < ITEMS; ++i) {
-    if (s + i < e) {
-      if (xa >= pm && xb >= pe) {
-        // pair exhausted at position s+i == pe: move to the pair that holds it
-        const int q = s + i;
-        int l2 = p + 1, h2 = npairs - 1;
-        while (l2 < h2) {
-          const int mid = (l2 + h2 + 1) >> 1;
-          if (pre[mid * span] <= q) {
-            l2 = mid;
-          } else {
-            h2 = mid - 1;
-          }
-        }
-        p = l2 < npairs - 1 ? l2 : npairs - 1;
-        ps = pre[p * span];
-        pm = pre[min(p * span + span / 2, nk)];
-        pe = pre[min(p * span + span, nk)];
-        xa = ps;
-        xb = pm;
-        ka = sk[xa];
-        kb = sk[xb];
-      }
-      const bool ta = (xb >= pe) || ((xa < pm) && !cmp(kb, ka));
-      ok[i] = ta ? ka : kb;
-      if constexpr (HasVal<V>::value) ov[i] = sv[ta ? xa : xb];
-      if (ta) {
-        ++xa;
-        ka = sk[xa];
-      } else {
-        ++xb;
-        kb = sk[xb];
-      }
+    if (c.exhausted()) {
+      // the pair ends at position s+i == pe: continue in the pair holding it
+      const int q = s + i;
+      p = find_pair(pre, npairs, span, q, p < npairs - 1 ? p + 1 : p);
+      ps = pre[p * span];
+      pm = pre[min(p * span + span / 2, nk)];
+      pe = pre[min(p * span + span, nk)];
+      c.init(sk, ps, pm, pm, pe, cmp);
     }
+    int src;
+    bool ta;
+    ok[i] = c.step(sk, cmp, src, ta);
+    if constexpr (HasVal<V>::value) ov[i] = sv[src];
   }
 }
 

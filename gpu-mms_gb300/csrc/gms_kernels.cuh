@@ -56,8 +56,8 @@ enum DeviceStatus : int { DEV_TILE_OVERFLOW = 1, DEV_BAD_SEGMENT = 2, DEV_COPY_T
 template <class KeyT, class V, int CAP>
 struct TileSmemLayout {
   static constexpr bool kHasVal = HasVal<V>::value;
-  static constexpr size_t key_bytes = ((sizeof(KeyT) * (CAP + 1) + 15) / 16) * 16;
-  static constexpr size_t val_bytes = kHasVal ? ((sizeof(V) * (CAP + 1) + 15) / 16) * 16 : 0;
+  static constexpr size_t key_bytes = ((sizeof(KeyT) * (CAP + 2) + 15) / 16) * 16;
+  static constexpr size_t val_bytes = kHasVal ? ((sizeof(V) * (CAP + 2) + 15) / 16) * 16 : 0;
   static constexpr int kMaxK = 32;
   static constexpr size_t pre_bytes = 16 * ((sizeof(int) * (kMaxK + 1) + 15) / 16);
   static constexpr size_t gs_bytes = sizeof(int64_t) * kMaxK;
@@ -327,10 +327,10 @@ struct MergeSmemLayout {
   static constexpr int kMaxK = 32;
   static constexpr size_t round16(size_t x) { return (x + 15) / 16 * 16; }
   // every segment region may add up to 30 bytes of alignment slack
-  static constexpr size_t stage_k_bytes = round16(sizeof(KeyT) * (CAP + 1) + 32 * kMaxK + 16);
-  static constexpr size_t stage_v_bytes = kHasVal ? round16(sizeof(V) * (CAP + 1) + 32 * kMaxK + 16) : 0;
-  static constexpr size_t mk_bytes = round16(sizeof(KeyT) * (CAP + 1));
-  static constexpr size_t mv_bytes = kHasVal ? round16(sizeof(V) * (CAP + 1)) : 0;
+  static constexpr size_t stage_k_bytes = round16(sizeof(KeyT) * (CAP + 2) + 32 * kMaxK + 16);
+  static constexpr size_t stage_v_bytes = kHasVal ? round16(sizeof(V) * (CAP + 2) + 32 * kMaxK + 16) : 0;
+  static constexpr size_t mk_bytes = round16(sizeof(KeyT) * (CAP + 2));
+  static constexpr size_t mv_bytes = kHasVal ? round16(sizeof(V) * (CAP + 2)) : 0;
   static constexpr size_t off_stage_v = stage_k_bytes;
   static constexpr size_t off_mk = off_stage_v + stage_v_bytes;
   static constexpr size_t off_mv = off_mk + mk_bytes;
@@ -559,67 +559,54 @@ __global__ void __launch_bounds__(NT, 2) merge_tiles_kernel(TileArgs<KeyT, V> a,
       const KeyT* sk = reinterpret_cast<const KeyT*>(stage_k);
       const V* sv = reinterpret_cast<const V*>(stage_v);
       const int npairs = (nk + 1) / 2;
-      int lo = 0, hi = npairs - 1;
-      while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (cpre[2 * mid] <= s) lo = mid; else hi = mid - 1;
-      }
-      int p = lo;
-      auto setup = [&](int pp, const KeyT*& A, const KeyT*& Bp, int& na, int& nb, int& base) {
-        const int ka = 2 * pp;
-        const int kb = min(2 * pp + 1, nk);
-        base = cpre[ka];
-        na = cpre[ka + 1] - cpre[ka];
-        nb = (kb < nk) ? cpre[kb + 1] - cpre[kb] : 0;
-        A = sk + sbk[ka];
-        Bp = (kb < nk) ? sk + sbk[kb] : A + na;
-      };
-      const KeyT* A;
-      const KeyT* Bq;
-      int na, nb, base;
-      setup(p, A, Bq, na, nb, base);
       const int enc = a.enc_on_load;
       const EncCmp<Cmp, Codec> ecmp{enc};
-      const int diag = s - base;
-      int ia = merge_path(A, na, Bq, nb, diag, ecmp);
-      int ib = diag - ia;
-      KeyT ka = maybe_enc<Codec>(A[ia], enc);
-      KeyT kb = maybe_enc<Codec>(Bq[ib], enc);
+      int p = find_pair(cpre, npairs, 2, s);
+      // segments 2p (A) and 2p+1 (B, may not exist) of the staged tile
+      int64_t offA = 0, offB = 0;  // value index = stage index + off (per side)
+      auto setup = [&](int pp, int diag, MergeCursor<KeyT>& c) {
+        const int ka_ = 2 * pp;
+        const int kb_ = min(2 * pp + 1, nk);
+        const int na = cpre[ka_ + 1] - cpre[ka_];
+        const int nb = (kb_ < nk) ? cpre[kb_ + 1] - cpre[kb_] : 0;
+        const int a0 = sbk[ka_];
+        const int b0 = (kb_ < nk) ? sbk[kb_] : a0 + na;
+        const int ia = diag > 0 ? merge_path(sk + a0, na, sk + b0, nb, diag, ecmp) : 0;
+        c.init(sk, a0 + ia, a0 + na, b0 + (diag - ia), b0 + nb, cmp);
+        if constexpr (kHasVal) {
+          if (a.gen_index) {
+            offA = gsrc[ka_] - a0;
+            offB = (kb_ < nk) ? gsrc[kb_] - b0 : 0;
+          } else {
+            offA = sbv[ka_] - a0;
+            offB = (kb_ < nk) ? sbv[kb_] - b0 : 0;
+          }
+        }
+      };
+      MergeCursor<KeyT> c;
+      setup(p, s - cpre[2 * p], c);
+      c.ka = maybe_enc<Codec>(c.ka, enc);
+      c.kb = maybe_enc<Codec>(c.kb, enc);
 #pragma unroll
       for (int i = 0; i < ITEMS; ++i) {
-        if (s + i < e) {
-          if (ia >= na && ib >= nb) {
-            const int q = s + i;
-            int l2 = p + 1, h2 = npairs - 1;
-            while (l2 < h2) {
-              const int mid = (l2 + h2 + 1) >> 1;
-              if (cpre[2 * mid] <= q) l2 = mid; else h2 = mid - 1;
-            }
-            p = l2 < npairs - 1 ? l2 : npairs - 1;
-            setup(p, A, Bq, na, nb, base);
-            ia = 0;
-            ib = 0;
-            ka = maybe_enc<Codec>(A[0], enc);
-            kb = maybe_enc<Codec>(Bq[0], enc);
-          }
-          const bool ta = (ib >= nb) || ((ia < na) && !cmp(kb, ka));
-          ok[i] = ta ? ka : kb;
-          if constexpr (kHasVal) {
-            const int seg = ta ? 2 * p : 2 * p + 1;
-            const int off = ta ? ia : ib;
-            if (a.gen_index) {
-              ov[i] = (V)(gsrc[seg] + off);
-            } else {
-              ov[i] = sv[sbv[seg] + off];
-            }
-          }
-          if (ta) {
-            ++ia;
-            ka = maybe_enc<Codec>(A[ia], enc);
-          } else {
-            ++ib;
-            kb = maybe_enc<Codec>(Bq[ib], enc);
-          }
+        if (c.exhausted()) {
+          p = find_pair(cpre, npairs, 2, s + i, p < npairs - 1 ? p + 1 : p);
+          setup(p, 0, c);
+          c.ka = maybe_enc<Codec>(c.ka, enc);
+          c.kb = maybe_enc<Codec>(c.kb, enc);
+        }
+        // the cursor step, with the codec applied to each freshly loaded key
+        const bool ta = (c.xb >= c.eb) || ((c.xa < c.ea) && !cmp(c.kb, c.ka));
+        ok[i] = ta ? c.ka : c.kb;
+        const int cur = ta ? c.xa : c.xb;
+        const KeyT nv = maybe_enc<Codec>(sk[cur + 1], enc);
+        c.xa = ta ? cur + 1 : c.xa;
+        c.xb = ta ? c.xb : cur + 1;
+        c.ka = ta ? nv : c.ka;
+        c.kb = ta ? c.kb : nv;
+        if constexpr (kHasVal) {
+          const int64_t vi = cur + (ta ? offA : offB);
+          ov[i] = a.gen_index ? (V)vi : sv[vi];
         }
       }
 #pragma unroll
@@ -672,11 +659,14 @@ __global__ void __launch_bounds__(NT, 2) merge_tiles_kernel(TileArgs<KeyT, V> a,
 // every run, merged in (key, run, block) order) is cut every G entries.  The
 // first key of block F[j*G] is boundary j.  One warp per boundary; lane k finds
 // how many keys of run k precede the boundary in the stable (key, run, index)
-// order by binary search over run k.  Between two boundaries every run
-// contributes at most (its blocks in that stretch of F + 1) blocks, so a tile
-// holds at most (G + K) * B keys.
+// order: first by binary search over run k's block sample `samp` (small and
+// cache-resident), which brackets the answer to one block, then inside that
+// block of the run.  Between two boundaries every run contributes at most
+// (its blocks in that stretch of F + 1) blocks, so a tile holds at most
+// (G + K) * B keys.
 template <class KeyT, class Cmp, class Codec>
-__global__ void __launch_bounds__(256) splitter_kernel(const KeyT* __restrict__ data, const KeyT* __restrict__ fkeys,
+__global__ void __launch_bounds__(256) splitter_kernel(const KeyT* __restrict__ data, const KeyT* __restrict__ samp,
+                                                        const KeyT* __restrict__ fkeys,
                                                         const uint32_t* __restrict__ fidx, int64_t n, int64_t L,
                                                         int k, int64_t sample_run_len, int sample_b, int64_t G,
                                                         int64_t tiles_full, int64_t tiles_last, int64_t groups,
@@ -712,22 +702,31 @@ __global__ void __launch_bounds__(256) splitter_kernel(const KeyT* __restrict__ 
       if (lane == kb) {
         c = ib;
       } else {
-        const KeyT* r = data + gbase + rs;
-        int64_t lo = 0, hi = len;
-        if (lane < kb) {
-          // keys <= v come first (earlier run wins ties)
-          while (lo < hi) {
-            const int64_t mid = (lo + hi) >> 1;
-            if (!cmp(v, maybe_enc<Codec>(r[mid], enc))) lo = mid + 1; else hi = mid;
-          }
-        } else {
-          // keys < v come first
-          while (lo < hi) {
-            const int64_t mid = (lo + hi) >> 1;
-            if (cmp(maybe_enc<Codec>(r[mid], enc), v)) lo = mid + 1; else hi = mid;
-          }
+        // earlier runs win ties: a key precedes the boundary if key <= v
+        // (lane < kb) or key < v (lane > kb)
+        const bool le = lane < kb;
+        auto precedes = [&](const KeyT& x) -> bool { return le ? !cmp(v, x) : cmp(x, v); };
+        // 1. blocks whose first key precedes the boundary
+        const KeyT* sr = samp + (g * (int64_t)k + lane) * sample_run_len;
+        const int64_t nb = (len + sample_b - 1) / sample_b;
+        int64_t lo = 0, hi = nb;
+        while (lo < hi) {
+          const int64_t mid = (lo + hi) >> 1;
+          if (precedes(sr[mid])) lo = mid + 1; else hi = mid;
         }
-        c = lo;
+        // 2. inside the last such block
+        if (lo == 0) {
+          c = 0;
+        } else {
+          const KeyT* r = data + gbase + rs;
+          int64_t a0 = (lo - 1) * sample_b + 1;
+          int64_t a1 = min64(lo * (int64_t)sample_b, len);
+          while (a0 < a1) {
+            const int64_t mid = (a0 + a1) >> 1;
+            if (precedes(maybe_enc<Codec>(r[mid], enc))) a0 = mid + 1; else a1 = mid;
+          }
+          c = a0;
+        }
       }
     }
     desc[row * k + lane] = c;

@@ -330,7 +330,7 @@ struct Engine {
       const int64_t threads = rows * 32;
       hook_before(KC_SPLIT, st);
       splitter_kernel<KeyT, Cmp, Codec><<<(unsigned)ceil_div(threads, 256), 256, 0, st>>>(
-          in, w.fk[level + 1], w.fi[level + 1], n, L, k, Ls, sb, G, tiles_full, tiles_last, groups, w.desc[level],
+          in, S, w.fk[level + 1], w.fi[level + 1], n, L, k, Ls, sb, G, tiles_full, tiles_last, groups, w.desc[level],
           w.doff[level], enc);
       e = cudaGetLastError();
       hook_after(KC_SPLIT, st);

@@ -85,10 +85,17 @@ def model_round(keys, idx, L, geo, stats, level=0):
                     assert 0 <= kb < k
                     if kk == kb:
                         c = ib
-                    elif kk < kb:
-                        c = int(np.searchsorted(run, v, side="right"))
                     else:
-                        c = int(np.searchsorted(run, v, side="left"))
+                        side = "right" if kk < kb else "left"
+                        # splitter_kernel: block sample first, then one block
+                        samp = S[(g * k + kk) * Ls:(g * k + kk) * Ls + ceil_div(lens[kk], B)]
+                        m = int(np.searchsorted(samp, v, side=side))
+                        if m == 0:
+                            c = 0
+                        else:
+                            a0, a1 = (m - 1) * B + 1, min(m * B, lens[kk])
+                            c = a0 + int(np.searchsorted(run[a0:a1], v, side=side))
+                        assert c == int(np.searchsorted(run, v, side=side))
                 desc[j, kk] = c
         doff = desc.sum(axis=1)
         for j in range(jg):
