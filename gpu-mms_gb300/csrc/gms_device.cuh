@@ -14,6 +14,8 @@
 #pragma once
 
 #include <cstdint>
+#include <utility>
+
 #include <cuda_runtime.h>
 
 namespace gms {
@@ -126,19 +128,14 @@ struct Batcher {
   static constexpr NetTable table = batcher_table(N);
 };
 
-template <int N, int C, class KeyT, class Cmp>
-__device__ __forceinline__ void network_apply(KeyT (&r)[N], Cmp cmp) {
-  if constexpr (C < Batcher<N>::table.n) {
-    constexpr int ia = Batcher<N>::table.a[C];
-    constexpr int ib = Batcher<N>::table.b[C];
-    cas(r[ia], r[ib], cmp);
-    network_apply<N, C + 1>(r, cmp);
-  }
+template <int N, class KeyT, class Cmp, int... I>
+__device__ __forceinline__ void network_apply(KeyT (&r)[N], Cmp cmp, std::integer_sequence<int, I...>) {
+  (cas(r[Batcher<N>::table.a[I]], r[Batcher<N>::table.b[I]], cmp), ...);
 }
 
 template <int N, class KeyT, class Cmp>
 __device__ __forceinline__ void network_sort(KeyT (&r)[N], Cmp cmp) {
-  network_apply<N, 0>(r, cmp);
+  network_apply<N>(r, cmp, std::make_integer_sequence<int, Batcher<N>::table.n>{});
 }
 
 // Odd-even transposition sort: only adjacent keys are exchanged, and only when
@@ -184,14 +181,17 @@ __device__ __forceinline__ int merge_path(const KeyT* a, int na, const KeyT* b, 
 }
 
 // Cursor of a stable two-way merge over shared memory.  A = [xa, ea),
-// B = [xb, eb) (absolute indices in one buffer); ka/kb hold the heads.  step()
-// emits the smaller head (A wins ties) and advances that side with a single
-// unconditional shared-memory load at index max+1 of the consumed side, which
-// is always inside the buffer (buffers carry one slack element).  No branches.
+// B = [xb, eb) (absolute indices in one buffer).  ka/kb hold the heads and
+// na_/nb_ the element after each head, so the shared-memory load issued by a
+// step (two past the consumed element) is only needed two steps later: the
+// load latency leaves the per-step dependency chain, which is then just
+// compare -> select.  step() emits the smaller head (A wins ties); no branches.
+// Loads may run up to two elements past a run end, so every buffer carries
+// slack elements.
 template <class KeyT>
 struct MergeCursor {
   int xa, ea, xb, eb;
-  KeyT ka, kb;
+  KeyT ka, kb, na_, nb_;
 
   template <class Cmp>
   __device__ __forceinline__ void init(const KeyT* sk, int a0, int a1, int b0, int b1, Cmp) {
@@ -200,7 +200,9 @@ struct MergeCursor {
     xb = b0;
     eb = b1;
     ka = sk[a0];
+    na_ = sk[a0 + 1];
     kb = sk[b0];
+    nb_ = sk[b0 + 1];
   }
 
   // Returns the emitted key; `src` receives its index, `took_a` its side.
@@ -209,11 +211,13 @@ struct MergeCursor {
     const bool ta = (xb >= eb) || ((xa < ea) && !cmp(kb, ka));
     const KeyT o = ta ? ka : kb;
     const int cur = ta ? xa : xb;
-    const KeyT nv = sk[cur + 1];
+    const KeyT far = sk[cur + 2];
+    ka = ta ? na_ : ka;
+    na_ = ta ? far : na_;
+    kb = ta ? kb : nb_;
+    nb_ = ta ? nb_ : far;
     xa = ta ? cur + 1 : xa;
     xb = ta ? xb : cur + 1;
-    ka = ta ? nv : ka;
-    kb = ta ? kb : nv;
     src = cur;
     took_a = ta;
     return o;
@@ -277,6 +281,17 @@ __device__ __forceinline__ void merge_level_var(const KeyT* sk, const V* sv, con
   const int ia = merge_path(sk + ps, pm - ps, sk + pm, pe - pm, diag, cmp);
   MergeCursor<KeyT> c;
   c.init(sk, ps + ia, pm, pm + (diag - ia), pe, cmp);
+  if (pe - s >= ITEMS) {
+    // common case: all ITEMS outputs come from this pair -- no per-step checks
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i) {
+      int src;
+      bool ta;
+      ok[i] = c.step(sk, cmp, src, ta);
+      if constexpr (HasVal<V>::value) ov[i] = sv[src];
+    }
+    return;
+  }
 #pragma unroll
   for (int i = 0; i < ITEMS; ++i) {
     if (c.exhausted()) {

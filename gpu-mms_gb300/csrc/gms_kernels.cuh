@@ -56,8 +56,8 @@ enum DeviceStatus : int { DEV_TILE_OVERFLOW = 1, DEV_BAD_SEGMENT = 2, DEV_COPY_T
 template <class KeyT, class V, int CAP>
 struct TileSmemLayout {
   static constexpr bool kHasVal = HasVal<V>::value;
-  static constexpr size_t key_bytes = ((sizeof(KeyT) * (CAP + 2) + 15) / 16) * 16;
-  static constexpr size_t val_bytes = kHasVal ? ((sizeof(V) * (CAP + 2) + 15) / 16) * 16 : 0;
+  static constexpr size_t key_bytes = ((sizeof(KeyT) * (CAP + 4) + 15) / 16) * 16;
+  static constexpr size_t val_bytes = kHasVal ? ((sizeof(V) * (CAP + 4) + 15) / 16) * 16 : 0;
   static constexpr int kMaxK = 32;
   static constexpr size_t pre_bytes = 16 * ((sizeof(int) * (kMaxK + 1) + 15) / 16);
   static constexpr size_t gs_bytes = sizeof(int64_t) * kMaxK;
@@ -327,10 +327,10 @@ struct MergeSmemLayout {
   static constexpr int kMaxK = 32;
   static constexpr size_t round16(size_t x) { return (x + 15) / 16 * 16; }
   // every segment region may add up to 30 bytes of alignment slack
-  static constexpr size_t stage_k_bytes = round16(sizeof(KeyT) * (CAP + 2) + 32 * kMaxK + 16);
-  static constexpr size_t stage_v_bytes = kHasVal ? round16(sizeof(V) * (CAP + 2) + 32 * kMaxK + 16) : 0;
-  static constexpr size_t mk_bytes = round16(sizeof(KeyT) * (CAP + 2));
-  static constexpr size_t mv_bytes = kHasVal ? round16(sizeof(V) * (CAP + 2)) : 0;
+  static constexpr size_t stage_k_bytes = round16(sizeof(KeyT) * (CAP + 4) + 32 * kMaxK + 16);
+  static constexpr size_t stage_v_bytes = kHasVal ? round16(sizeof(V) * (CAP + 4) + 32 * kMaxK + 16) : 0;
+  static constexpr size_t mk_bytes = round16(sizeof(KeyT) * (CAP + 4));
+  static constexpr size_t mv_bytes = kHasVal ? round16(sizeof(V) * (CAP + 4)) : 0;
   static constexpr size_t off_stage_v = stage_k_bytes;
   static constexpr size_t off_mk = off_stage_v + stage_v_bytes;
   static constexpr size_t off_mv = off_mk + mk_bytes;
@@ -584,26 +584,32 @@ __global__ void __launch_bounds__(NT, 2) merge_tiles_kernel(TileArgs<KeyT, V> a,
         }
       };
       MergeCursor<KeyT> c;
+      auto enc_heads = [&]() {
+        c.ka = maybe_enc<Codec>(c.ka, enc);
+        c.na_ = maybe_enc<Codec>(c.na_, enc);
+        c.kb = maybe_enc<Codec>(c.kb, enc);
+        c.nb_ = maybe_enc<Codec>(c.nb_, enc);
+      };
       setup(p, s - cpre[2 * p], c);
-      c.ka = maybe_enc<Codec>(c.ka, enc);
-      c.kb = maybe_enc<Codec>(c.kb, enc);
+      enc_heads();
 #pragma unroll
       for (int i = 0; i < ITEMS; ++i) {
         if (c.exhausted()) {
           p = find_pair(cpre, npairs, 2, s + i, p < npairs - 1 ? p + 1 : p);
           setup(p, 0, c);
-          c.ka = maybe_enc<Codec>(c.ka, enc);
-          c.kb = maybe_enc<Codec>(c.kb, enc);
+          enc_heads();
         }
         // the cursor step, with the codec applied to each freshly loaded key
         const bool ta = (c.xb >= c.eb) || ((c.xa < c.ea) && !cmp(c.kb, c.ka));
         ok[i] = ta ? c.ka : c.kb;
         const int cur = ta ? c.xa : c.xb;
-        const KeyT nv = maybe_enc<Codec>(sk[cur + 1], enc);
+        const KeyT far = maybe_enc<Codec>(sk[cur + 2], enc);
+        c.ka = ta ? c.na_ : c.ka;
+        c.na_ = ta ? far : c.na_;
+        c.kb = ta ? c.kb : c.nb_;
+        c.nb_ = ta ? c.nb_ : far;
         c.xa = ta ? cur + 1 : c.xa;
         c.xb = ta ? c.xb : cur + 1;
-        c.ka = ta ? nv : c.ka;
-        c.kb = ta ? c.kb : nv;
         if constexpr (kHasVal) {
           const int64_t vi = cur + (ta ? offA : offB);
           ov[i] = a.gen_index ? (V)vi : sv[vi];
