@@ -163,61 +163,76 @@ __device__ __forceinline__ void transposition_sort(KeyT (&r)[N], V (&v)[N], Cmp 
 }
 
 // ---------------------------------------------------------------------------
-// Merge path: number of elements of `a` among the first `diag` outputs of the
-// stable merge of a and b (a wins ties).  Lower-bound search whose steps are
-// branch-free (selects), so lanes of a warp never diverge inside a step.
-template <class KeyT, class Cmp>
-__device__ __forceinline__ int merge_path(const KeyT* a, int na, const KeyT* b, int nb, int diag, Cmp cmp) {
-  int lo = diag - nb > 0 ? diag - nb : 0;
-  int len = (diag < na ? diag : na) - lo;
+// Shared-memory loaders.  PlainLoad reads keys as stored; EncLoad applies the
+// codec (used when a merge reads raw user keys straight from a staging buffer).
+template <class KeyT>
+struct PlainLoad {
+  const KeyT* base;
+  __device__ __forceinline__ KeyT operator()(int i) const { return base[i]; }
+};
+template <class KeyT, class Codec>
+struct EncLoad {
+  const KeyT* base;
+  int on;
+  __device__ __forceinline__ KeyT operator()(int i) const {
+    const KeyT x = base[i];
+    return on ? Codec::enc(x) : x;
+  }
+};
+
+// Merge path over [lo, hi]: number of elements of A = [a0, a0+na) among the
+// first `diag` outputs of the stable merge of A and B = [b0, b0+nb) (A wins
+// ties), searched only inside [lo, hi].  Branch-free steps.
+template <class Ld, class Cmp>
+__device__ __forceinline__ int merge_path_in(const Ld& ld, int a0, int b0, int diag, int lo, int hi, Cmp cmp) {
+  int len = hi - lo;
   while (len > 0) {
     const int half = len >> 1;
     const int mid = lo + half;
-    const bool go = !cmp(b[diag - 1 - mid], a[mid]);
+    const bool go = !cmp(ld(b0 + diag - 1 - mid), ld(a0 + mid));
     lo = go ? mid + 1 : lo;
     len = go ? len - half - 1 : half;
   }
   return lo;
 }
 
-// Cursor of a stable two-way merge over shared memory.  A = [xa, ea),
-// B = [xb, eb) (absolute indices in one buffer).  ka/kb hold the heads and
-// na_/nb_ the element after each head, so the shared-memory load issued by a
-// step (two past the consumed element) is only needed two steps later: the
-// load latency leaves the per-step dependency chain, which is then just
-// compare -> select.  step() emits the smaller head (A wins ties); no branches.
-// Loads may run up to two elements past a run end, so every buffer carries
-// slack elements.
+template <class Ld, class Cmp>
+__device__ __forceinline__ int merge_path(const Ld& ld, int a0, int na, int b0, int nb, int diag, Cmp cmp) {
+  const int lo = diag - nb > 0 ? diag - nb : 0;
+  const int hi = diag < na ? diag : na;
+  return merge_path_in(ld, a0, b0, diag, lo, hi, cmp);
+}
+
+// Cursor of a stable two-way merge.  A = [xa, ea), B = [xb, eb) (absolute
+// indices of one buffer); ka/kb are the heads.  step() emits the smaller head
+// (A wins ties) and advances that side with one unconditional load at the
+// consumed index + 1 (buffers carry slack elements, so this stays in bounds).
+// No branches.
 template <class KeyT>
 struct MergeCursor {
   int xa, ea, xb, eb;
-  KeyT ka, kb, na_, nb_;
+  KeyT ka, kb;
 
-  template <class Cmp>
-  __device__ __forceinline__ void init(const KeyT* sk, int a0, int a1, int b0, int b1, Cmp) {
+  template <class Ld>
+  __device__ __forceinline__ void init(const Ld& ld, int a0, int a1, int b0, int b1) {
     xa = a0;
     ea = a1;
     xb = b0;
     eb = b1;
-    ka = sk[a0];
-    na_ = sk[a0 + 1];
-    kb = sk[b0];
-    nb_ = sk[b0 + 1];
+    ka = ld(a0);
+    kb = ld(b0);
   }
 
-  // Returns the emitted key; `src` receives its index, `took_a` its side.
-  template <class Cmp>
-  __device__ __forceinline__ KeyT step(const KeyT* sk, Cmp cmp, int& src, bool& took_a) {
+  template <class Ld, class Cmp>
+  __device__ __forceinline__ KeyT step(const Ld& ld, Cmp cmp, int& src, bool& took_a) {
     const bool ta = (xb >= eb) || ((xa < ea) && !cmp(kb, ka));
     const KeyT o = ta ? ka : kb;
     const int cur = ta ? xa : xb;
-    const KeyT far = sk[cur + 2];
-    ka = ta ? na_ : ka;
-    na_ = ta ? far : na_;
-    kb = ta ? kb : nb_;
-    nb_ = ta ? nb_ : far;
+    const KeyT nv = ld(cur + 1);
     xa = ta ? cur + 1 : xa;
     xb = ta ? xb : cur + 1;
+    ka = ta ? nv : ka;
+    kb = ta ? kb : nv;
     src = cur;
     took_a = ta;
     return o;
@@ -226,89 +241,106 @@ struct MergeCursor {
   __device__ __forceinline__ bool exhausted() const { return xa + xb == ea + eb; }
 };
 
-// One level of pairwise merging over runs of equal length `rl` inside a
-// shared-memory tile of `cap` keys.  Thread `t` produces outputs
-// [t*ITEMS, t*ITEMS + ITEMS) into registers.  ITEMS divides rl, so a thread
-// never straddles two pairs.
-template <int ITEMS, class KeyT, class V, class Cmp>
-__device__ __forceinline__ void merge_level_regular(const KeyT* sk, const V* sv, int cap, int rl, int s,
-                                                    KeyT (&ok)[ITEMS], V (&ov)[ITEMS], Cmp cmp) {
-  const int ps = (s / (2 * rl)) * (2 * rl);
-  const int pm = min(ps + rl, cap);
-  const int pe = min(ps + 2 * rl, cap);
-  const int diag = s - ps;
-  const int ia = merge_path(sk + ps, pm - ps, sk + pm, pe - pm, diag, cmp);
+// One merge pair of a level: its first output position and its two runs.
+struct PairRange {
+  int out0;    // output position of the pair's first element
+  int a0, ea;  // run A (absolute buffer indices)
+  int b0, eb;  // run B
+  int id;      // pair index (for payload lookups)
+};
+
+// Produces the ITEMS outputs [s, s+ITEMS) of one merge level.
+//   pair_of(q)          -> PairRange of the pair holding output position q
+//   emit(i, key, src, ta, pair) stores output i
+// When all ITEMS outputs lie in one pair (the common case) the thread runs two
+// independent merge streams (outputs [s, s+H) and [s+H, s+ITEMS)), so two
+// dependency chains are in flight; the second stream's merge-path search only
+// scans the H+1 candidates after the first's co-rank.  Otherwise a single
+// stream walks across pair ends.  Positions past the valid outputs produce
+// garbage that the caller never reads.
+template <int ITEMS, class KeyT, class Ld, class Cmp, class PairOf, class Emit>
+__device__ __forceinline__ void merge_thread(int s, const Ld& ld, Cmp cmp, const PairOf& pair_of, const Emit& emit) {
+  constexpr int H = (ITEMS + 1) / 2;
+  PairRange P = pair_of(s);
+  const int na = P.ea - P.a0, nb = P.eb - P.b0;
+  const int diag = s - P.out0;
+  if (na + nb - diag >= ITEMS) {
+    const int ia1 = merge_path(ld, P.a0, na, P.b0, nb, diag, cmp);
+    const int d2 = diag + H;
+    int lo2 = d2 - nb > ia1 ? d2 - nb : ia1;
+    int hi2 = ia1 + H;
+    hi2 = hi2 < na ? hi2 : na;
+    hi2 = hi2 < d2 ? hi2 : d2;
+    const int ia2 = merge_path_in(ld, P.a0, P.b0, d2, lo2, hi2, cmp);
+    MergeCursor<KeyT> c1, c2;
+    c1.init(ld, P.a0 + ia1, P.ea, P.b0 + (diag - ia1), P.eb);
+    c2.init(ld, P.a0 + ia2, P.ea, P.b0 + (d2 - ia2), P.eb);
+#pragma unroll
+    for (int i = 0; i < H; ++i) {
+      int src1;
+      bool ta1;
+      const KeyT o1 = c1.step(ld, cmp, src1, ta1);
+      emit(i, o1, src1, ta1, P);
+      if (H + i < ITEMS) {
+        int src2;
+        bool ta2;
+        const KeyT o2 = c2.step(ld, cmp, src2, ta2);
+        emit(H + i, o2, src2, ta2, P);
+      }
+    }
+    return;
+  }
+  const int ia = merge_path(ld, P.a0, na, P.b0, nb, diag, cmp);
   MergeCursor<KeyT> c;
-  c.init(sk, ps + ia, pm, pm + (diag - ia), pe, cmp);
+  c.init(ld, P.a0 + ia, P.ea, P.b0 + (diag - ia), P.eb);
 #pragma unroll
   for (int i = 0; i < ITEMS; ++i) {
+    if (c.exhausted()) {
+      P = pair_of(s + i);
+      c.init(ld, P.a0, P.ea, P.b0, P.eb);
+    }
     int src;
     bool ta;
-    ok[i] = c.step(sk, cmp, src, ta);
-    if constexpr (HasVal<V>::value) ov[i] = sv[src];
+    const KeyT o = c.step(ld, cmp, src, ta);
+    emit(i, o, src, ta, P);
   }
 }
 
-// Locates the pair of level `span` that holds output position q: the largest
-// pair index whose start pre[p*span] is <= q.
-__device__ __forceinline__ int find_pair(const int* pre, int npairs, int span, int q, int lo = 0) {
-  int hi = npairs - 1;
+// Largest pair index p (< npairs) whose start pre[p*span] is <= q.
+__device__ __forceinline__ int find_pair(const int* pre, int npairs, int span, int q) {
+  int lo = 0, hi = npairs - 1;
   while (lo < hi) {
     const int mid = (lo + hi + 1) >> 1;
-    lo = (pre[mid * span] <= q) ? mid : lo;
-    hi = (pre[mid * span] <= q) ? hi : mid - 1;
+    const bool le = pre[mid * span] <= q;
+    lo = le ? mid : lo;
+    hi = le ? hi : mid - 1;
   }
   return lo;
 }
 
-// One level of pairwise merging over nk variable-length runs whose boundaries
-// are pre[0..nk] (pre[nk] = total).  At level `span` (2, 4, 8, ...) the runs
-// [pre[p*span], pre[p*span+span/2]) and [pre[p*span+span/2], pre[p*span+span])
-// are merged.  Runs may be empty.  A thread whose outputs reach the end of its
-// pair continues with the next non-empty pair (rare; a uniform branch).  All
-// ITEMS steps run; outputs past the tile end are garbage the caller does not
-// write back.
-template <int ITEMS, class KeyT, class V, class Cmp>
-__device__ __forceinline__ void merge_level_var(const KeyT* sk, const V* sv, const int* pre, int nk, int span,
-                                                int s, int e, KeyT (&ok)[ITEMS], V (&ov)[ITEMS], Cmp cmp) {
-  (void)e;
-  const int npairs = (nk + span - 1) / span;
-  int p = find_pair(pre, npairs, span, s);
-  int ps = pre[p * span];
-  int pm = pre[min(p * span + span / 2, nk)];
-  int pe = pre[min(p * span + span, nk)];
-  const int diag = s - ps;
-  const int ia = merge_path(sk + ps, pm - ps, sk + pm, pe - pm, diag, cmp);
-  MergeCursor<KeyT> c;
-  c.init(sk, ps + ia, pm, pm + (diag - ia), pe, cmp);
-  if (pe - s >= ITEMS) {
-    // common case: all ITEMS outputs come from this pair -- no per-step checks
-#pragma unroll
-    for (int i = 0; i < ITEMS; ++i) {
-      int src;
-      bool ta;
-      ok[i] = c.step(sk, cmp, src, ta);
-      if constexpr (HasVal<V>::value) ov[i] = sv[src];
-    }
-    return;
+// Pair lookup for a level of `span` over compact runs with boundaries pre[].
+struct CompactPairs {
+  const int* pre;
+  int nk, span, npairs;
+  __device__ __forceinline__ PairRange operator()(int q) const {
+    const int p = find_pair(pre, npairs, span, q);
+    const int ps = pre[p * span];
+    const int pm = pre[min(p * span + span / 2, nk)];
+    const int pe = pre[min(p * span + span, nk)];
+    return PairRange{ps, ps, pm, pm, pe, p};
   }
-#pragma unroll
-  for (int i = 0; i < ITEMS; ++i) {
-    if (c.exhausted()) {
-      // the pair ends at position s+i == pe: continue in the pair holding it
-      const int q = s + i;
-      p = find_pair(pre, npairs, span, q, p < npairs - 1 ? p + 1 : p);
-      ps = pre[p * span];
-      pm = pre[min(p * span + span / 2, nk)];
-      pe = pre[min(p * span + span, nk)];
-      c.init(sk, ps, pm, pm, pe, cmp);
-    }
-    int src;
-    bool ta;
-    ok[i] = c.step(sk, cmp, src, ta);
-    if constexpr (HasVal<V>::value) ov[i] = sv[src];
+};
+
+// Pair lookup for equal runs of length rl inside a tile of cap keys.
+struct RegularPairs {
+  int rl, cap;
+  __device__ __forceinline__ PairRange operator()(int q) const {
+    const int ps = (q / (2 * rl)) * (2 * rl);
+    const int pm = min(ps + rl, cap);
+    const int pe = min(ps + 2 * rl, cap);
+    return PairRange{ps, ps, pm, pm, pe, ps / (2 * rl)};
   }
-}
+};
 
 // Largest element (under cmp) across the block; every thread gets it.
 // `scratch` holds NT keys.  Shared-memory tree, so any copyable key type works

@@ -56,12 +56,18 @@ enum DeviceStatus : int { DEV_TILE_OVERFLOW = 1, DEV_BAD_SEGMENT = 2, DEV_COPY_T
 template <class KeyT, class V, int CAP>
 struct TileSmemLayout {
   static constexpr bool kHasVal = HasVal<V>::value;
+  static constexpr int kMaxK = 32;
+  // two ping-pong key buffers (+ payload), each with slack elements
   static constexpr size_t key_bytes = ((sizeof(KeyT) * (CAP + 4) + 15) / 16) * 16;
   static constexpr size_t val_bytes = kHasVal ? ((sizeof(V) * (CAP + 4) + 15) / 16) * 16 : 0;
-  static constexpr int kMaxK = 32;
   static constexpr size_t pre_bytes = 16 * ((sizeof(int) * (kMaxK + 1) + 15) / 16);
   static constexpr size_t gs_bytes = sizeof(int64_t) * kMaxK;
-  static constexpr size_t bytes = key_bytes + val_bytes + pre_bytes + gs_bytes;
+  static constexpr size_t off_k1 = key_bytes;
+  static constexpr size_t off_v0 = 2 * key_bytes;
+  static constexpr size_t off_v1 = off_v0 + val_bytes;
+  static constexpr size_t off_pre = off_v1 + val_bytes;
+  static constexpr size_t off_gs = off_pre + pre_bytes;
+  static constexpr size_t bytes = off_gs + gs_bytes;
 };
 
 __device__ __forceinline__ int64_t min64(int64_t a, int64_t b) { return a < b ? a : b; }
@@ -100,23 +106,26 @@ template <class KeyT, class V, class Cmp, class Codec, int MODE, bool STABLE, in
 __global__ void __launch_bounds__(NT) tile_kernel(TileArgs<KeyT, V> a) {
   constexpr int CAP = NT * ITEMS;
   constexpr bool kHasVal = HasVal<V>::value;
-  using L = TileSmemLayout<KeyT, V, CAP>;
+  using Lay = TileSmemLayout<KeyT, V, CAP>;
   extern __shared__ __align__(16) unsigned char smem[];
-  KeyT* sk = reinterpret_cast<KeyT*>(smem);
-  V* sv = reinterpret_cast<V*>(smem + L::key_bytes);
-  int* pre = reinterpret_cast<int*>(smem + L::key_bytes + L::val_bytes);
-  int64_t* gs = reinterpret_cast<int64_t*>(smem + L::key_bytes + L::val_bytes + L::pre_bytes);
+  KeyT* const k0 = reinterpret_cast<KeyT*>(smem);
+  KeyT* const k1 = reinterpret_cast<KeyT*>(smem + Lay::off_k1);
+  V* const v0 = reinterpret_cast<V*>(smem + Lay::off_v0);
+  V* const v1 = reinterpret_cast<V*>(smem + Lay::off_v1);
+  int* pre = reinterpret_cast<int*>(smem + Lay::off_pre);
+  int64_t* gs = reinterpret_cast<int64_t*>(smem + Lay::off_gs);
   const Cmp cmp;
   const int tid = threadIdx.x;
+  KeyT* sk = k0;
+  V* sv = v0;
 
   int64_t out_base;   // global index of this tile's first output
   int64_t run_base;   // global index of the output run this tile belongs to
   int64_t run_index;  // index of that output run
   int cnt;            // keys in this tile
   int nk = 1;         // runs in the tile (GROUP/TILE)
-
-  KeyT ok[ITEMS];
-  V ov[ITEMS];
+  int cur = 0;        // buffer holding the current level's input
+  const int s = tid * ITEMS;
 
   if constexpr (MODE == MODE_BASE) {
     const int64_t base = (int64_t)blockIdx.x * a.L;
@@ -125,7 +134,6 @@ __global__ void __launch_bounds__(NT) tile_kernel(TileArgs<KeyT, V> a) {
     out_base = base;
     run_base = base;
     run_index = blockIdx.x;
-    // Coalesced striped load: register i of thread t holds element t + i*NT.
     KeyT r[ITEMS];
     V rv[ITEMS];
     if constexpr (STABLE) {
@@ -152,7 +160,7 @@ __global__ void __launch_bounds__(NT) tile_kernel(TileArgs<KeyT, V> a) {
         for (int i = 1; i < ITEMS; ++i) {
           if (tid * ITEMS + i < cnt) m = cmp(m, r[i]) ? r[i] : m;
         }
-        __syncthreads();  // every chunk is in registers; sk is free as scratch
+        __syncthreads();  // every chunk is in registers; the buffer is free as scratch
         m = block_max<NT>(m, sk, cmp);
 #pragma unroll
         for (int i = 0; i < ITEMS; ++i) {
@@ -162,12 +170,14 @@ __global__ void __launch_bounds__(NT) tile_kernel(TileArgs<KeyT, V> a) {
       transposition_sort<ITEMS>(r, rv, cmp);
       __syncthreads();
     } else {
+      // Coalesced striped load: register i of thread t holds element t + i*NT.
 #pragma unroll
       for (int i = 0; i < ITEMS; ++i) {
         const int p = tid + i * NT;
         if (p < cnt) r[i] = maybe_enc<Codec>(a.in[base + p], a.enc_on_load);
       }
       if (cnt < CAP) {
+        // a short last tile is padded with copies of its largest key
         KeyT m = r[0];
         if (tid >= cnt) m = maybe_enc<Codec>(a.in[base], a.enc_on_load);
 #pragma unroll
@@ -186,21 +196,24 @@ __global__ void __launch_bounds__(NT) tile_kernel(TileArgs<KeyT, V> a) {
     // ITEMS is odd, so the ITEMS-strided stores hit distinct banks.
 #pragma unroll
     for (int i = 0; i < ITEMS; ++i) {
-      sk[tid * ITEMS + i] = r[i];
-      if constexpr (kHasVal) sv[tid * ITEMS + i] = rv[i];
+      sk[s + i] = r[i];
+      if constexpr (kHasVal) sv[s + i] = rv[i];
     }
     __syncthreads();
-    // Merge levels up to the whole (padded) tile.
-    const int s = tid * ITEMS;
+    // Merge levels up to the whole (padded) tile, ping-ponging the buffers.
     for (int rl = ITEMS; rl < CAP; rl *= 2) {
-      merge_level_regular<ITEMS>(sk, sv, CAP, rl, s, ok, ov, cmp);
+      const KeyT* xk = (cur ? k1 : k0);
+      KeyT* yk = (cur ? k0 : k1);
+      const V* xv = (cur ? v1 : v0);
+      V* yv = (cur ? v0 : v1);
+      const PlainLoad<KeyT> ld{xk};
+      const RegularPairs pairs{rl, CAP};
+      merge_thread<ITEMS, KeyT>(s, ld, cmp, pairs, [&](int i, KeyT k, int src, bool, const PairRange&) {
+        yk[s + i] = k;
+        if constexpr (kHasVal) yv[s + i] = xv[src];
+      });
       __syncthreads();
-#pragma unroll
-      for (int i = 0; i < ITEMS; ++i) {
-        sk[s + i] = ok[i];
-        if constexpr (kHasVal) sv[s + i] = ov[i];
-      }
-      __syncthreads();
+      cur ^= 1;
     }
   } else {
     // ---- GROUP / TILE: gather the K input segments into shared memory ----
@@ -277,50 +290,52 @@ __global__ void __launch_bounds__(NT) tile_kernel(TileArgs<KeyT, V> a) {
     run_base = gbase;
     run_index = g;
     __syncthreads();
-    // ---- ceil(log2 nk) levels of pairwise merging ----
-    const int s = tid * ITEMS;
-    const int e = min(s + ITEMS, cnt);
+    // ---- ceil(log2 nk) levels of pairwise merging, ping-ponging ----
     for (int span = 2; span < 2 * nk; span *= 2) {
-      if (s < cnt) merge_level_var<ITEMS>(sk, sv, pre, nk, span, s, e, ok, ov, cmp);
-      __syncthreads();
+      const KeyT* xk = (cur ? k1 : k0);
+      KeyT* yk = (cur ? k0 : k1);
+      const V* xv = (cur ? v1 : v0);
+      V* yv = (cur ? v0 : v1);
       if (s < cnt) {
-#pragma unroll
-        for (int i = 0; i < ITEMS; ++i) {
-          if (s + i < e) {
-            sk[s + i] = ok[i];
-            if constexpr (kHasVal) sv[s + i] = ov[i];
-          }
-        }
+        const PlainLoad<KeyT> ld{xk};
+        const CompactPairs pairs{pre, nk, span, (nk + span - 1) / span};
+        merge_thread<ITEMS, KeyT>(s, ld, cmp, pairs, [&](int i, KeyT k, int src, bool, const PairRange&) {
+          yk[s + i] = k;
+          if constexpr (kHasVal) yv[s + i] = xv[src];
+        });
       }
       __syncthreads();
+      cur ^= 1;
     }
   }
 
   // ---- coalesced store of the merged tile (+ block sample) ----
+  const KeyT* fk = (cur ? k1 : k0);
+  const V* fv = (cur ? v1 : v0);
   for (int p = tid; p < cnt; p += NT) {
-    a.out[out_base + p] = maybe_dec<Codec>(sk[p], a.dec_on_store);
-    if constexpr (kHasVal) a.vout[out_base + p] = sv[p];
+    a.out[out_base + p] = maybe_dec<Codec>(fk[p], a.dec_on_store);
+    if constexpr (kHasVal) a.vout[out_base + p] = fv[p];
   }
   if (a.sample_out) {
     // output positions whose offset in the output run is a multiple of B
     const int64_t rel0 = out_base - run_base;
     const int64_t first = (a.sample_b - rel0 % a.sample_b) % a.sample_b;
     for (int64_t p = first + (int64_t)tid * a.sample_b; p < cnt; p += (int64_t)NT * a.sample_b) {
-      a.sample_out[run_index * a.sample_run_len + (rel0 + p) / a.sample_b] = sk[p];
+      a.sample_out[run_index * a.sample_run_len + (rel0 + p) / a.sample_b] = fk[p];
     }
   }
 }
 
 // ---------------------------------------------------------------------------
-// Persistent K-way merge of forecast tiles with bulk-copy staging.
+// K-way merge of one forecast tile per CTA, staged with bulk copies.
 //
-// Each CTA walks tiles blockIdx.x, blockIdx.x + gridDim.x, ...  For each tile,
-// warp 0 places the K run segments in the staging buffer (16-byte-aligned
-// regions) and issues one cp.async.bulk per segment, completing on an
-// mbarrier.  The first merge level reads the staged segments directly and
-// writes the merged pairs to the merge buffer; the staging buffer is then free
-// and warp 0 immediately issues the NEXT tile's copies, which land while the
-// remaining ceil(log2 K)-1 levels and the store of the current tile run.
+// Warp 0 places the K run segments of the tile in the staging buffer
+// (16-byte-aligned regions) and issues one cp.async.bulk per segment,
+// completing on an mbarrier transaction count.  The first merge level reads
+// the staged segment pairs directly; the remaining ceil(log2 K)-1 levels
+// ping-pong between the merge buffer and the (now free) staging buffer.  Three
+// CTAs of 512 threads fit an SM for 4-byte keys, so one CTA's copy latency is
+// covered by the others' merging.
 template <class KeyT, class V, int CAP>
 struct MergeSmemLayout {
   static constexpr bool kHasVal = HasVal<V>::value;
@@ -335,63 +350,55 @@ struct MergeSmemLayout {
   static constexpr size_t off_mk = off_stage_v + stage_v_bytes;
   static constexpr size_t off_mv = off_mk + mk_bytes;
   static constexpr size_t off_desc = off_mv + mv_bytes;
-  // descriptors, double-buffered: cpre[2][33] int, sbk[2][32] int, sbv[2][32] int,
-  // gsrc[2][32] int64, meta[2][4] int64, bar (8 bytes)
-  static constexpr size_t desc_bytes = 2 * (33 + 32 + 32) * 4 + 4 + 2 * 32 * 8 + 2 * 4 * 8 + 16;
-  static constexpr size_t bytes = off_desc + desc_bytes;
+  // cpre[33] int, sbk[32] int, sbv[32] int, (pad), gsrc[32] int64, meta[4] int64, bar
+  static constexpr size_t off_gsrc = off_desc + 4 * (33 + 32 + 32) + 4;
+  static constexpr size_t off_meta = off_gsrc + 8 * 32;
+  static constexpr size_t off_bar = off_meta + 8 * 4;
+  static constexpr size_t bytes = off_bar + 16;
 };
 
 template <class KeyT, class V, class Cmp, class Codec, int NT, int ITEMS>
-__global__ void __launch_bounds__(NT, 2) merge_tiles_kernel(TileArgs<KeyT, V> a, int64_t total_tiles) {
+__global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, int64_t total_tiles) {
   constexpr int CAP = NT * ITEMS;
   constexpr bool kHasVal = HasVal<V>::value;
   using Lay = MergeSmemLayout<KeyT, V, CAP>;
-  constexpr int kMaxK = Lay::kMaxK;
+  static_assert(Lay::off_gsrc % 8 == 0, "descriptor alignment");
   extern __shared__ __align__(16) unsigned char smem[];
   unsigned char* stage_k = smem;
   unsigned char* stage_v = smem + Lay::off_stage_v;
-  KeyT* mk = reinterpret_cast<KeyT*>(smem + Lay::off_mk);
-  V* mv = reinterpret_cast<V*>(smem + Lay::off_mv);
-  int* cpre_all = reinterpret_cast<int*>(smem + Lay::off_desc);  // [2][33]
-  int* sbk_all = cpre_all + 2 * 33;                                // [2][32]
-  int* sbv_all = sbk_all + 2 * 32;                                 // [2][32]
-  int64_t* gsrc_all = reinterpret_cast<int64_t*>(smem + Lay::off_desc + ((2 * 97 * 4 + 4 + 7) / 8) * 8);
-  int64_t* meta_all = gsrc_all + 2 * 32;  // [2][4]: out_base, run_base, run_index, cnt|bad
-  uint64_t* bar = reinterpret_cast<uint64_t*>(meta_all + 2 * 4);
+  KeyT* const k0 = reinterpret_cast<KeyT*>(stage_k);
+  KeyT* const k1 = reinterpret_cast<KeyT*>(smem + Lay::off_mk);
+  V* const v0 = reinterpret_cast<V*>(stage_v);
+  V* const v1 = reinterpret_cast<V*>(smem + Lay::off_mv);
+  int* cpre = reinterpret_cast<int*>(smem + Lay::off_desc);
+  int* sbk = cpre + 33;
+  int* sbv = sbk + 32;
+  int64_t* gsrc = reinterpret_cast<int64_t*>(smem + Lay::off_gsrc);
+  int64_t* meta = reinterpret_cast<int64_t*>(smem + Lay::off_meta);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + Lay::off_bar);
   const Cmp cmp;
   const int tid = threadIdx.x;
   const int lane = tid & 31;
   const int nk = a.k;
-  const uint64_t arr_k_lo = reinterpret_cast<uint64_t>(a.in);
-  const uint64_t arr_k_hi = arr_k_lo + (uint64_t)a.n * sizeof(KeyT);
-  uint64_t arr_v_lo = 0, arr_v_hi = 0;
-  if constexpr (kHasVal) {
-    if (!a.gen_index) {
-      arr_v_lo = reinterpret_cast<uint64_t>(a.vin);
-      arr_v_hi = arr_v_lo + (uint64_t)a.n * sizeof(V);
-    }
-  }
 
-  auto tile_valid = [&](int64_t tau) -> bool {
-    if (tau >= total_tiles) return false;
-    const int64_t g = tau / a.tiles_full;
-    const int64_t j = tau - g * a.tiles_full;
-    const int64_t jg = (g == a.groups - 1) ? a.tiles_last : a.tiles_full;
-    return j < jg;
-  };
-  auto next_tile = [&](int64_t tau) -> int64_t {
-    tau += gridDim.x;
-    while (tau < total_tiles && !tile_valid(tau)) tau += gridDim.x;
-    return tau;
-  };
+  const int64_t tau = blockIdx.x;
+  if (tau >= total_tiles) return;
+  const int64_t g = tau / a.tiles_full;
+  const int64_t j = tau - g * a.tiles_full;
+  const int64_t jg = (g == a.groups - 1) ? a.tiles_last : a.tiles_full;
+  if (j >= jg) return;
 
-  // Warp 0: place and issue the copies of tile `tau` into descriptor slot d.
-  auto issue = [&](int64_t tau, int d) {
-    const int64_t g = tau / a.tiles_full;
-    const int64_t j = tau - g * a.tiles_full;
+  if (tid == 0) mbar_init(bar, 1);
+  fence_mbar_init();
+  __syncthreads();
+
+  // ---- warp 0: place the segments and issue their copies ----
+  if (tid < 32) {
     const int64_t gbase = g * a.L * a.k;
     const int64_t row = g * (a.tiles_full + 1) + j;
     const int64_t ng = min64(a.L * a.k, a.n - gbase);
+    const uint64_t arr_k_lo = reinterpret_cast<uint64_t>(a.in);
+    const uint64_t arr_k_hi = arr_k_lo + (uint64_t)a.n * sizeof(KeyT);
     int len = 0;
     int64_t gs = 0;
     bool bad = false;
@@ -403,7 +410,6 @@ __global__ void __launch_bounds__(NT, 2) merge_tiles_kernel(TileArgs<KeyT, V> a,
       len = bad ? 0 : (int)(hi - lo);
       gs = gbase + (int64_t)lane * a.L + (bad ? 0 : lo);
     }
-    // compact prefix of lengths
     int incl = len;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -412,7 +418,6 @@ __global__ void __launch_bounds__(NT, 2) merge_tiles_kernel(TileArgs<KeyT, V> a,
     }
     const int total = __shfl_sync(0xffffffffu, incl, 31);
     const bool any_bad = __any_sync(0xffffffffu, bad) || total > CAP;
-    int* cpre = cpre_all + d * 33;
     if (lane < nk) cpre[lane + 1] = incl;
     if (lane == 0) cpre[0] = 0;
     // key regions
@@ -430,9 +435,13 @@ __global__ void __launch_bounds__(NT, 2) merge_tiles_kernel(TileArgs<KeyT, V> a,
     uint32_t bulk = (!any_bad && ck.be > ck.bs) ? (uint32_t)(ck.be - ck.bs) : 0u;
     SegCopy cv{};
     uint32_t off_v = 0;
+    uint64_t Av = 0;
+    const bool carry = kHasVal && !a.gen_index;
     if constexpr (kHasVal) {
-      if (!a.gen_index) {
-        const uint64_t Av = arr_v_lo + (uint64_t)gs * sizeof(V);
+      if (carry) {
+        const uint64_t arr_v_lo = reinterpret_cast<uint64_t>(a.vin);
+        const uint64_t arr_v_hi = arr_v_lo + (uint64_t)a.n * sizeof(V);
+        Av = arr_v_lo + (uint64_t)gs * sizeof(V);
         const uint64_t Ev = Av + (uint64_t)len * sizeof(V);
         cv = seg_copy(Av, Ev, arr_v_lo, arr_v_hi);
         const uint32_t reg_v = (uint32_t)(cv.e16 - cv.a16);
@@ -450,23 +459,17 @@ __global__ void __launch_bounds__(NT, 2) merge_tiles_kernel(TileArgs<KeyT, V> a,
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) tx += __shfl_xor_sync(0xffffffffu, tx, o);
     if (lane < nk) {
-      sbk_all[d * 32 + lane] = (int)((off_k + (uint32_t)(A - ck.a16)) / sizeof(KeyT));
-      gsrc_all[d * 32 + lane] = gs;
-      if constexpr (kHasVal) {
-        if (!a.gen_index) {
-          sbv_all[d * 32 + lane] = (int)((off_v + (uint32_t)((arr_v_lo + (uint64_t)gs * sizeof(V)) - cv.a16)) / sizeof(V));
-        }
-      }
+      sbk[lane] = (int)((off_k + (uint32_t)(A - ck.a16)) / sizeof(KeyT));
+      gsrc[lane] = gs;
+      if (carry) sbv[lane] = (int)((off_v + (uint32_t)(Av - cv.a16)) / sizeof(V));
     }
     if (lane == 0) {
-      int64_t* meta = meta_all + d * 4;
       meta[0] = gbase + a.doff[row];
       meta[1] = gbase;
       meta[2] = g;
       meta[3] = any_bad ? -1 : total;
       if (any_bad && a.err) atomicOr(a.err, DEV_BAD_SEGMENT);
     }
-    // staging buffers were read by the generic proxy; order before bulk writes
     fence_proxy_async_smem();
     if (lane == 0) mbar_arrive_expect_tx(bar, tx);
     __syncwarp();
@@ -475,23 +478,21 @@ __global__ void __launch_bounds__(NT, 2) merge_tiles_kernel(TileArgs<KeyT, V> a,
       if (ck.be > ck.bs) {
         bulk_g2s(dstk + (ck.bs - ck.a16), reinterpret_cast<const void*>(ck.bs), (uint32_t)(ck.be - ck.bs), bar);
       }
-      // plain loads for the bytes outside the array's aligned interior
+      // plain loads for bytes outside the array's 16-byte-aligned interior
+      // (never more than 15 bytes at each end of the array)
       const KeyT* src = a.in + gs;
       KeyT* dst = reinterpret_cast<KeyT*>(dstk + (A - ck.a16));
       for (int i = 0; i < len; ++i) {
         const uint64_t addr = A + (uint64_t)i * sizeof(KeyT);
-        const bool in_bulk = (ck.be > ck.bs) && addr >= ck.bs && addr < ck.be;
-        if (!in_bulk) dst[i] = src[i];
         if (ck.be > ck.bs && addr >= ck.bs && addr < ck.be) {
-          // skip the bulk interior in one step
-          const int64_t skip = (int64_t)((ck.be - addr) / sizeof(KeyT)) - 1;
-          i += (int)skip;
+          i += (int)((ck.be - addr) / sizeof(KeyT)) - 1;  // skip the bulk interior
+        } else {
+          dst[i] = src[i];
         }
       }
       if constexpr (kHasVal) {
-        if (!a.gen_index) {
+        if (carry) {
           unsigned char* dstv = stage_v + off_v;
-          const uint64_t Av = arr_v_lo + (uint64_t)gs * sizeof(V);
           if (cv.be > cv.bs) {
             bulk_g2s(dstv + (cv.bs - cv.a16), reinterpret_cast<const void*>(cv.bs), (uint32_t)(cv.be - cv.bs), bar);
           }
@@ -499,162 +500,91 @@ __global__ void __launch_bounds__(NT, 2) merge_tiles_kernel(TileArgs<KeyT, V> a,
           V* vdst = reinterpret_cast<V*>(dstv + (Av - cv.a16));
           for (int i = 0; i < len; ++i) {
             const uint64_t addr = Av + (uint64_t)i * sizeof(V);
-            const bool in_bulk = (cv.be > cv.bs) && addr >= cv.bs && addr < cv.be;
-            if (!in_bulk) vdst[i] = vsrc[i];
-            if (in_bulk) {
-              const int64_t skip = (int64_t)((cv.be - addr) / sizeof(V)) - 1;
-              i += (int)skip;
+            if (cv.be > cv.bs && addr >= cv.bs && addr < cv.be) {
+              i += (int)((cv.be - addr) / sizeof(V)) - 1;
+            } else {
+              vdst[i] = vsrc[i];
             }
           }
         }
       }
     }
-  };
+  }
 
-  if (tid == 0) mbar_init(bar, 1);
-  fence_mbar_init();
-  __syncthreads();
-
-  int64_t tau = blockIdx.x;
-  while (tau < total_tiles && !tile_valid(tau)) tau += gridDim.x;
-  if (tau >= total_tiles) return;
-  if (tid < 32) issue(tau, 0);
-  uint32_t phase = 0;
-  int d = 0;
+  // ---- wait for the staged segments (bounded) ----
   constexpr uint32_t kSpinLimit = 1u << 26;
+  if (!mbar_wait_bounded(bar, 0, kSpinLimit)) {
+    if (tid == 0 && a.err) atomicOr(a.err, DEV_COPY_TIMEOUT);
+    mbar_wait_bounded(bar, 0, kSpinLimit);  // let copies in flight land
+    return;
+  }
+  __syncthreads();  // plain-loaded bytes from warp 0 are visible
+  const int cnt = (int)meta[3];
+  if (cnt < 0) return;  // rejected tile (never expected): nothing was copied
+  const int64_t out_base = meta[0];
+  const int64_t run_base = meta[1];
+  const int64_t run_index = meta[2];
+  const int s = tid * ITEMS;
 
-  while (tau < total_tiles) {
-    // ---- wait for this tile's staged segments ----
-    if (!mbar_wait_bounded(bar, phase, kSpinLimit)) {
-      if (tid == 0 && a.err) atomicOr(a.err, DEV_COPY_TIMEOUT);
-      mbar_wait_bounded(bar, phase, kSpinLimit);  // let copies in flight land
-      return;
-    }
-    phase ^= 1u;
-    __syncthreads();  // plain-loaded bytes from warp 0 are visible
-    const int* cpre = cpre_all + d * 33;
-    const int64_t* meta = meta_all + d * 4;
-    const int cnt = (int)meta[3];
-    const int64_t out_base = meta[0];
-    const int64_t run_base = meta[1];
-    const int64_t run_index = meta[2];
-    const int64_t next = next_tile(tau);
-    if (cnt < 0) {
-      // rejected tile (never expected): skip it, keep the pipeline going
-      __syncthreads();
-      if (next < total_tiles && tid < 32) issue(next, d ^ 1);
-      tau = next;
-      d ^= 1;
-      continue;
-    }
-    const int s = tid * ITEMS;
-    const int e = min(s + ITEMS, cnt);
-    KeyT ok[ITEMS];
-    V ov[ITEMS];
-    // ---- level 1: staged segment pairs -> merge buffer ----
+  // ---- level 1: staged segment pairs -> merge buffer ----
+  if (s < cnt) {
+    const int npairs = (nk + 1) / 2;
+    const EncLoad<KeyT, Codec> ld{reinterpret_cast<const KeyT*>(stage_k), a.enc_on_load};
+    auto pair_of = [&](int q) -> PairRange {
+      const int p = find_pair(cpre, npairs, 2, q);
+      const int ka_ = 2 * p;
+      const int kb_ = min(2 * p + 1, nk);
+      const int na = cpre[ka_ + 1] - cpre[ka_];
+      const int nb = (kb_ < nk) ? cpre[kb_ + 1] - cpre[kb_] : 0;
+      const int a0 = sbk[ka_];
+      const int b0 = (kb_ < nk) ? sbk[kb_] : a0 + na;
+      return PairRange{cpre[ka_], a0, a0 + na, b0, b0 + nb, p};
+    };
+    KeyT* yk = k1;
+    V* yv = v1;
+    const V* sv = reinterpret_cast<const V*>(stage_v);
+    const int gen = a.gen_index;
+    merge_thread<ITEMS, KeyT>(s, ld, cmp, pair_of, [&](int i, KeyT k, int src, bool ta, const PairRange& P) {
+      yk[s + i] = k;
+      if constexpr (kHasVal) {
+        const int seg = ta ? 2 * P.id : 2 * P.id + 1;
+        const int off = src - sbk[seg];
+        yv[s + i] = gen ? (V)(gsrc[seg] + off) : sv[sbv[seg] + off];
+      }
+    });
+  }
+  __syncthreads();
+  int cur = 1;
+  // ---- remaining levels: merge buffer <-> staging buffer ----
+  for (int span = 4; span < 2 * nk; span *= 2) {
+    const KeyT* xk = (cur ? k1 : k0);
+    KeyT* yk = (cur ? k0 : k1);
+    const V* xv = (cur ? v1 : v0);
+    V* yv = (cur ? v0 : v1);
     if (s < cnt) {
-      const int* sbk = sbk_all + d * 32;
-      const int* sbv = sbv_all + d * 32;
-      const int64_t* gsrc = gsrc_all + d * 32;
-      const KeyT* sk = reinterpret_cast<const KeyT*>(stage_k);
-      const V* sv = reinterpret_cast<const V*>(stage_v);
-      const int npairs = (nk + 1) / 2;
-      const int enc = a.enc_on_load;
-      const EncCmp<Cmp, Codec> ecmp{enc};
-      int p = find_pair(cpre, npairs, 2, s);
-      // segments 2p (A) and 2p+1 (B, may not exist) of the staged tile
-      int64_t offA = 0, offB = 0;  // value index = stage index + off (per side)
-      auto setup = [&](int pp, int diag, MergeCursor<KeyT>& c) {
-        const int ka_ = 2 * pp;
-        const int kb_ = min(2 * pp + 1, nk);
-        const int na = cpre[ka_ + 1] - cpre[ka_];
-        const int nb = (kb_ < nk) ? cpre[kb_ + 1] - cpre[kb_] : 0;
-        const int a0 = sbk[ka_];
-        const int b0 = (kb_ < nk) ? sbk[kb_] : a0 + na;
-        const int ia = diag > 0 ? merge_path(sk + a0, na, sk + b0, nb, diag, ecmp) : 0;
-        c.init(sk, a0 + ia, a0 + na, b0 + (diag - ia), b0 + nb, cmp);
-        if constexpr (kHasVal) {
-          if (a.gen_index) {
-            offA = gsrc[ka_] - a0;
-            offB = (kb_ < nk) ? gsrc[kb_] - b0 : 0;
-          } else {
-            offA = sbv[ka_] - a0;
-            offB = (kb_ < nk) ? sbv[kb_] - b0 : 0;
-          }
-        }
-      };
-      MergeCursor<KeyT> c;
-      auto enc_heads = [&]() {
-        c.ka = maybe_enc<Codec>(c.ka, enc);
-        c.na_ = maybe_enc<Codec>(c.na_, enc);
-        c.kb = maybe_enc<Codec>(c.kb, enc);
-        c.nb_ = maybe_enc<Codec>(c.nb_, enc);
-      };
-      setup(p, s - cpre[2 * p], c);
-      enc_heads();
-#pragma unroll
-      for (int i = 0; i < ITEMS; ++i) {
-        if (c.exhausted()) {
-          p = find_pair(cpre, npairs, 2, s + i, p < npairs - 1 ? p + 1 : p);
-          setup(p, 0, c);
-          enc_heads();
-        }
-        // the cursor step, with the codec applied to each freshly loaded key
-        const bool ta = (c.xb >= c.eb) || ((c.xa < c.ea) && !cmp(c.kb, c.ka));
-        ok[i] = ta ? c.ka : c.kb;
-        const int cur = ta ? c.xa : c.xb;
-        const KeyT far = maybe_enc<Codec>(sk[cur + 2], enc);
-        c.ka = ta ? c.na_ : c.ka;
-        c.na_ = ta ? far : c.na_;
-        c.kb = ta ? c.kb : c.nb_;
-        c.nb_ = ta ? c.nb_ : far;
-        c.xa = ta ? cur + 1 : c.xa;
-        c.xb = ta ? c.xb : cur + 1;
-        if constexpr (kHasVal) {
-          const int64_t vi = cur + (ta ? offA : offB);
-          ov[i] = a.gen_index ? (V)vi : sv[vi];
-        }
-      }
-#pragma unroll
-      for (int i = 0; i < ITEMS; ++i) {
-        if (s + i < e) {
-          mk[s + i] = ok[i];
-          if constexpr (kHasVal) mv[s + i] = ov[i];
-        }
-      }
+      const PlainLoad<KeyT> ld{xk};
+      const CompactPairs pairs{cpre, nk, span, (nk + span - 1) / span};
+      merge_thread<ITEMS, KeyT>(s, ld, cmp, pairs, [&](int i, KeyT k, int src, bool, const PairRange&) {
+        yk[s + i] = k;
+        if constexpr (kHasVal) yv[s + i] = xv[src];
+      });
     }
-    __syncthreads();  // merge buffer complete; staging buffer free
-    if (next < total_tiles && tid < 32) issue(next, d ^ 1);
-    // ---- remaining levels inside the merge buffer ----
-    for (int span = 4; span < 2 * nk; span *= 2) {
-      if (s < cnt) merge_level_var<ITEMS>(mk, mv, cpre, nk, span, s, e, ok, ov, cmp);
-      __syncthreads();
-      if (s < cnt) {
-#pragma unroll
-        for (int i = 0; i < ITEMS; ++i) {
-          if (s + i < e) {
-            mk[s + i] = ok[i];
-            if constexpr (kHasVal) mv[s + i] = ov[i];
-          }
-        }
-      }
-      __syncthreads();
+    __syncthreads();
+    cur ^= 1;
+  }
+  // ---- coalesced store (+ block sample for the next round) ----
+  const KeyT* fk = (cur ? k1 : k0);
+  const V* fv = (cur ? v1 : v0);
+  for (int q = tid; q < cnt; q += NT) {
+    a.out[out_base + q] = maybe_dec<Codec>(fk[q], a.dec_on_store);
+    if constexpr (kHasVal) a.vout[out_base + q] = fv[q];
+  }
+  if (a.sample_out) {
+    const int64_t rel0 = out_base - run_base;
+    const int64_t first = (a.sample_b - rel0 % a.sample_b) % a.sample_b;
+    for (int64_t q = first + (int64_t)tid * a.sample_b; q < cnt; q += (int64_t)NT * a.sample_b) {
+      a.sample_out[run_index * a.sample_run_len + (rel0 + q) / a.sample_b] = fk[q];
     }
-    // ---- coalesced store (+ block sample for the next round) ----
-    for (int q = tid; q < cnt; q += NT) {
-      a.out[out_base + q] = maybe_dec<Codec>(mk[q], a.dec_on_store);
-      if constexpr (kHasVal) a.vout[out_base + q] = mv[q];
-    }
-    if (a.sample_out) {
-      const int64_t rel0 = out_base - run_base;
-      const int64_t first = (a.sample_b - rel0 % a.sample_b) % a.sample_b;
-      for (int64_t q = first + (int64_t)tid * a.sample_b; q < cnt; q += (int64_t)NT * a.sample_b) {
-        a.sample_out[run_index * a.sample_run_len + (rel0 + q) / a.sample_b] = mk[q];
-      }
-    }
-    __syncthreads();  // merge buffer free for the next tile
-    tau = next;
-    d ^= 1;
   }
 }
 

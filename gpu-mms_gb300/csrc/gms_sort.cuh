@@ -251,21 +251,19 @@ struct Engine {
     return e;
   }
 
-  // Persistent bulk-copy merge of the forecast tiles of one round.
+  // Bulk-copy merge of the forecast tiles of one round (one CTA per tile).
   template <class VV>
   static cudaError_t launch_merge_tiles(const TileArgs<KeyT, VV>& a, int64_t total_tiles, cudaStream_t st,
                                         int level) {
     if (total_tiles <= 0) return cudaSuccess;
+    if (total_tiles > 0x7fffffff) return cudaErrorInvalidConfiguration;
     auto kern = merge_tiles_kernel<KeyT, VV, Cmp, Codec, NT, ITEMS>;
     const size_t smem = MergeSmemLayout<KeyT, VV, CAP>::bytes;
     cudaError_t e = ensure_smem((const void*)kern, smem);
     if (e != cudaSuccess) return e;
-    const int pg = persistent_grid((const void*)kern, NT, smem, &e);
-    if (e != cudaSuccess) return e;
-    const int64_t grid = total_tiles < pg ? total_tiles : pg;
     const int kc = level == 0 ? KC_MERGE : KC_SAMPLE_MERGE;
     hook_before(kc, st);
-    kern<<<(unsigned)grid, NT, smem, st>>>(a, total_tiles);
+    kern<<<(unsigned)total_tiles, NT, smem, st>>>(a, total_tiles);
     e = cudaGetLastError();
     hook_after(kc, st);
     return e;
