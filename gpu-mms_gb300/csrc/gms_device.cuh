@@ -14,6 +14,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cstring>
 #include <utility>
 
 #include <cuda_runtime.h>
@@ -163,21 +164,74 @@ __device__ __forceinline__ void transposition_sort(KeyT (&r)[N], V (&v)[N], Cmp 
 }
 
 // ---------------------------------------------------------------------------
-// Shared-memory loaders.  PlainLoad reads keys as stored; EncLoad applies the
-// codec (used when a merge reads raw user keys straight from a staging buffer).
+// Shared-memory access through 32-bit shared-window addresses.  For 4- and
+// 8-byte keys the loads are explicit ld.shared (no generic 64-bit address
+// arithmetic); other types use ordinary accesses.
+template <class T>
+__device__ __forceinline__ T lds(uint32_t addr) {
+  if constexpr (sizeof(T) == 4) {
+    uint32_t v;
+    asm("ld.shared.b32 %0, [%1];" : "=r"(v) : "r"(addr));
+    T t;
+    memcpy(&t, &v, 4);
+    return t;
+  } else if constexpr (sizeof(T) == 8) {
+    unsigned long long v;
+    asm("ld.shared.b64 %0, [%1];" : "=l"(v) : "r"(addr));
+    T t;
+    memcpy(&t, &v, 8);
+    return t;
+  } else {
+    T t;
+    // any other size: an ordinary access through a shared pointer
+    const unsigned char* p = static_cast<const unsigned char*>(__cvta_shared_to_generic(addr));
+    memcpy(&t, p, sizeof(T));
+    return t;
+  }
+}
+
+template <class T>
+__device__ __forceinline__ void sts(uint32_t addr, const T& x) {
+  if constexpr (sizeof(T) == 4) {
+    uint32_t v;
+    memcpy(&v, &x, 4);
+    asm volatile("st.shared.b32 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
+  } else if constexpr (sizeof(T) == 8) {
+    unsigned long long v;
+    memcpy(&v, &x, 8);
+    asm volatile("st.shared.b64 [%0], %1;" ::"r"(addr), "l"(v) : "memory");
+  } else {
+    unsigned char* p = static_cast<unsigned char*>(__cvta_shared_to_generic(addr));
+    memcpy(p, &x, sizeof(T));
+  }
+}
+
+// Loaders.  PlainLoad reads keys as stored; EncLoad applies the codec (used
+// when a merge reads raw user keys straight from a staging buffer).
 template <class KeyT>
 struct PlainLoad {
-  const KeyT* base;
-  __device__ __forceinline__ KeyT operator()(int i) const { return base[i]; }
+  uint32_t base;  // shared-window byte address of element 0
+  __device__ __forceinline__ explicit PlainLoad(const KeyT* p) : base(static_cast<uint32_t>(__cvta_generic_to_shared(p))) {}
+  __device__ __forceinline__ KeyT operator()(int i) const { return lds<KeyT>(base + (uint32_t)i * (uint32_t)sizeof(KeyT)); }
 };
 template <class KeyT, class Codec>
 struct EncLoad {
-  const KeyT* base;
+  uint32_t base;
   int on;
+  __device__ __forceinline__ EncLoad(const KeyT* p, int on_) : base(static_cast<uint32_t>(__cvta_generic_to_shared(p))), on(on_) {}
   __device__ __forceinline__ KeyT operator()(int i) const {
-    const KeyT x = base[i];
+    const KeyT x = lds<KeyT>(base + (uint32_t)i * (uint32_t)sizeof(KeyT));
     return on ? Codec::enc(x) : x;
   }
+};
+
+// Shared-memory store helper with a fixed base.
+template <class T>
+struct SmemArray {
+  uint32_t base;
+  __device__ __forceinline__ explicit SmemArray(const T* p) : base(static_cast<uint32_t>(__cvta_generic_to_shared(p))) {}
+  __device__ __forceinline__ void put(int i, const T& x) const { sts<T>(base + (uint32_t)i * (uint32_t)sizeof(T), x); }
+  __device__ __forceinline__ T get(int i) const { return lds<T>(base + (uint32_t)i * (uint32_t)sizeof(T)); }
 };
 
 // Merge path over [lo, hi]: number of elements of A = [a0, a0+na) among the

@@ -103,7 +103,8 @@ struct EncCmp {
 // STABLE: equivalent keys keep their input order (used for key/value sorts and
 // for user comparators whose equivalent keys may differ in their bits).
 template <class KeyT, class V, class Cmp, class Codec, int MODE, bool STABLE, int NT, int ITEMS>
-__global__ void __launch_bounds__(NT) tile_kernel(TileArgs<KeyT, V> a) {
+__global__ void __launch_bounds__(NT, (MODE == MODE_BASE && sizeof(KeyT) == 4 && !HasVal<V>::value) ? 3 : 1)
+    tile_kernel(TileArgs<KeyT, V> a) {
   constexpr int CAP = NT * ITEMS;
   constexpr bool kHasVal = HasVal<V>::value;
   using Lay = TileSmemLayout<KeyT, V, CAP>;
@@ -206,11 +207,13 @@ __global__ void __launch_bounds__(NT) tile_kernel(TileArgs<KeyT, V> a) {
       KeyT* yk = (cur ? k0 : k1);
       const V* xv = (cur ? v1 : v0);
       V* yv = (cur ? v0 : v1);
-      const PlainLoad<KeyT> ld{xk};
+      const PlainLoad<KeyT> ld(xk);
+      const SmemArray<KeyT> yka(yk + s);
+      const SmemArray<V> xva(xv), yva(yv + s);
       const RegularPairs pairs{rl, CAP};
       merge_thread<ITEMS, KeyT>(s, ld, cmp, pairs, [&](int i, KeyT k, int src, bool, const PairRange&) {
-        yk[s + i] = k;
-        if constexpr (kHasVal) yv[s + i] = xv[src];
+        yka.put(i, k);
+        if constexpr (kHasVal) yva.put(i, xva.get(src));
       });
       __syncthreads();
       cur ^= 1;
@@ -297,11 +300,13 @@ __global__ void __launch_bounds__(NT) tile_kernel(TileArgs<KeyT, V> a) {
       const V* xv = (cur ? v1 : v0);
       V* yv = (cur ? v0 : v1);
       if (s < cnt) {
-        const PlainLoad<KeyT> ld{xk};
+        const PlainLoad<KeyT> ld(xk);
+        const SmemArray<KeyT> yka(yk + s);
+        const SmemArray<V> xva(xv), yva(yv + s);
         const CompactPairs pairs{pre, nk, span, (nk + span - 1) / span};
         merge_thread<ITEMS, KeyT>(s, ld, cmp, pairs, [&](int i, KeyT k, int src, bool, const PairRange&) {
-          yk[s + i] = k;
-          if constexpr (kHasVal) yv[s + i] = xv[src];
+          yka.put(i, k);
+          if constexpr (kHasVal) yva.put(i, xva.get(src));
         });
       }
       __syncthreads();
@@ -529,7 +534,7 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
   // ---- level 1: staged segment pairs -> merge buffer ----
   if (s < cnt) {
     const int npairs = (nk + 1) / 2;
-    const EncLoad<KeyT, Codec> ld{reinterpret_cast<const KeyT*>(stage_k), a.enc_on_load};
+    const EncLoad<KeyT, Codec> ld(reinterpret_cast<const KeyT*>(stage_k), a.enc_on_load);
     auto pair_of = [&](int q) -> PairRange {
       const int p = find_pair(cpre, npairs, 2, q);
       const int ka_ = 2 * p;
@@ -540,16 +545,16 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
       const int b0 = (kb_ < nk) ? sbk[kb_] : a0 + na;
       return PairRange{cpre[ka_], a0, a0 + na, b0, b0 + nb, p};
     };
-    KeyT* yk = k1;
-    V* yv = v1;
-    const V* sv = reinterpret_cast<const V*>(stage_v);
+    const SmemArray<KeyT> yka(k1 + s);
+    const SmemArray<V> yva(v1 + s);
+    const SmemArray<V> sva(reinterpret_cast<const V*>(stage_v));
     const int gen = a.gen_index;
     merge_thread<ITEMS, KeyT>(s, ld, cmp, pair_of, [&](int i, KeyT k, int src, bool ta, const PairRange& P) {
-      yk[s + i] = k;
+      yka.put(i, k);
       if constexpr (kHasVal) {
         const int seg = ta ? 2 * P.id : 2 * P.id + 1;
         const int off = src - sbk[seg];
-        yv[s + i] = gen ? (V)(gsrc[seg] + off) : sv[sbv[seg] + off];
+        yva.put(i, gen ? (V)(gsrc[seg] + off) : sva.get(sbv[seg] + off));
       }
     });
   }
@@ -562,11 +567,13 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
     const V* xv = (cur ? v1 : v0);
     V* yv = (cur ? v0 : v1);
     if (s < cnt) {
-      const PlainLoad<KeyT> ld{xk};
+      const PlainLoad<KeyT> ld(xk);
+      const SmemArray<KeyT> yka(yk + s);
+      const SmemArray<V> xva(xv), yva(yv + s);
       const CompactPairs pairs{cpre, nk, span, (nk + span - 1) / span};
       merge_thread<ITEMS, KeyT>(s, ld, cmp, pairs, [&](int i, KeyT k, int src, bool, const PairRange&) {
-        yk[s + i] = k;
-        if constexpr (kHasVal) yv[s + i] = xv[src];
+        yka.put(i, k);
+        if constexpr (kHasVal) yva.put(i, xva.get(src));
       });
     }
     __syncthreads();

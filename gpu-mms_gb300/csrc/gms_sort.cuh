@@ -168,6 +168,9 @@ inline cudaError_t ensure_smem(const void* kern, size_t bytes) {
   }
   e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
   if (e != cudaSuccess) return e;
+  // largest shared-memory carveout, so several tile CTAs fit an SM
+  e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  if (e != cudaSuccess) return e;
   if (nseen < 256) {
     seen_k[nseen] = kern;
     seen_d[nseen] = dev;
