@@ -46,6 +46,7 @@ int run_sort(K* in, V* vin, K* out, V* vout, int64_t n, cudaStream_t st) {
   if (n > ((int64_t)1 << 32) * 32) return set_error(GMS_ERR_TOO_LARGE, "n beyond 2^37");
   const gms::Tune t = default_tune();
   const gms::WsLayout l = Eng::plan(n, t);
+  if (!l.ok) return set_error(GMS_ERR_INVALID, "tuning too fine for this n (sample recursion too deep)");
   const size_t bytes = gms::ws_bytes_for<K>(l, t.k);
   int status = GMS_OK;
   void* ws = cache_get(0, bytes, st, &status);

@@ -49,6 +49,7 @@ int gms_merge_level_i32(const int32_t* in, int32_t* out, int64_t n, int64_t run_
   gms::Tune t = default_tune();
   t.k = k;
   const gms::WsLayout l = EngI32::plan_merge_level(n, run_len, t);
+  if (!l.ok) return set_error(GMS_ERR_INVALID, "tuning too fine for this n (sample recursion too deep)");
   int status = GMS_OK;
   void* ws = cache_get(0, gms::ws_bytes_for<uint32_t>(l, k), (cudaStream_t)st, &status);
   if (status != GMS_OK) return status;
@@ -77,6 +78,7 @@ int gms_find_partitions_i32(const int32_t* task, int64_t size, int k, int64_t ta
   cudaError_t e = cudaSuccess;
   if (task_size > 0) {
     const gms::WsLayout l = EngI32::plan_merge_level(task_size, size, t);
+    if (!l.ok) return set_error(GMS_ERR_INVALID, "tuning too fine for this task (sample recursion too deep)");
     void* ws = cache_get(0, gms::ws_bytes_for<uint32_t>(l, t.k), st, &status);
     if (status != GMS_OK) return status;
     const gms::WsPtrs<uint32_t> w = gms::ws_carve<uint32_t>(l, t.k, ws);

@@ -49,6 +49,7 @@ int gms_merge_level_u64(const uint64_t* in, uint64_t* out, int64_t n, int64_t ru
   gms::Tune t = default_tune();
   t.k = k;
   const gms::WsLayout l = EngU64::plan_merge_level(n, run_len, t);
+  if (!l.ok) return set_error(GMS_ERR_INVALID, "tuning too fine for this n (sample recursion too deep)");
   int status = GMS_OK;
   void* ws = cache_get(0, gms::ws_bytes_for<uint64_t>(l, k), (cudaStream_t)st, &status);
   if (status != GMS_OK) return status;

@@ -167,8 +167,8 @@ void gms_release_workspaces(void) {
 int gms_set_tune(int k, int sample_b, int bulk_copy) {
   clear_error();
   if (k < 2 || k > 32) return set_error(GMS_ERR_INVALID, "k must be in [2, 32]");
-  if (sample_b < 1 || (int64_t)kNT * kItems / sample_b - k < 1)
-    return set_error(GMS_ERR_INVALID, "sample_b leaves no room for a tile (need CAP/sample_b > k)");
+  if (sample_b < 8 || (int64_t)kNT * kItems / sample_b - k < 1)
+    return set_error(GMS_ERR_INVALID, "sample_b must be >= 8 and leave room for a tile (CAP/sample_b > k)");
   std::lock_guard<std::mutex> g(g_tune_mu);
   g_tune.k = k;
   g_tune.sample_b = sample_b;

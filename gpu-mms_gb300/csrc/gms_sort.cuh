@@ -74,6 +74,7 @@ struct WsLayout {
   int64_t f[kMaxLevels] = {0};         // merged samples (keys + index), level >= 1
   int64_t rows[kMaxLevels] = {0};      // tile boundary rows, level >= 0
   int depth = 0;
+  bool ok = true;                      // false: the recursion would exceed kMaxLevels
 };
 
 template <class KeyT>
@@ -201,6 +202,10 @@ struct Engine {
   static void plan_round(WsLayout& l, int level, int64_t n, int64_t L, const Tune& t, bool gather0 = false) {
     const int k = t.k;
     if ((int64_t)k * L <= CAP) return;  // GROUP mode, no scratch
+    if (level + 1 >= kMaxLevels) {
+      l.ok = false;  // sample recursion too deep for this tuning
+      return;
+    }
     const int sb = t.sample_b;
     const int64_t G = CAP / sb - k;
     const int64_t runs = ceil_div(n, L);

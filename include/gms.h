@@ -178,7 +178,9 @@ int gms_timing_reset(void);
  * (scripts/findK.sh, scripts/blocksThreads.sh).
  *   k          fan-in of a merge round, 2..32 (default 32)
  *   sample_b   block size of the forecast sample that cuts tiles (default 32;
- *              needs max_tile/sample_b > k)
+ *              8 <= sample_b and max_tile/sample_b > k).  A sort whose sample
+ *              recursion would get too deep for the tuning returns
+ *              GMS_ERR_INVALID.
  *   bulk_copy  1: persistent merge kernel staging segments with cp.async.bulk
  *              (default); 0: one CTA per tile with plain loads
  * ------------------------------------------------------------------------- */
