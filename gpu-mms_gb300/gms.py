@@ -28,7 +28,7 @@ INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC"]
-UNITS = ["gms_capi_misc.cu", "gms_capi_k32.cu", "gms_capi_k64.cu", "gms_capi_kv.cu"]
+UNITS = ["gms_capi_misc.cu", "gms_capi_k32.cu", "gms_capi_k64.cu", "gms_capi_kv.cu", "gms_capi_noalloc.cu"]
 
 GMS_OK = 0
 DTYPES = {"int32": 0, "uint32": 1, "float32": 2, "int64": 3, "uint64": 4, "float64": 5}
@@ -107,6 +107,7 @@ SIGNATURES = {
     "gms_sort_kv_u64_i32": (_i32, [_vp, _vp, _vp, _vp, _i64, _i32, _vp]),
     "gms_sort_kv_f64_i32": (_i32, [_vp, _vp, _vp, _vp, _i64, _i32, _vp]),
     "gms_sort_host_i32": (_i32, [_vp, _vp, _i64, _vp]),
+    "gms_sort_i32_noalloc": (_i32, [_vp, _vp, _i64, _vp]),
     "gms_sort_host_kv_u64_i32": (_i32, [_vp, _vp, _vp, _vp, _i64, _vp]),
     "gms_tile_sort_i32": (_i32, [_vp, _i64, _i64, _vp]),
     "gms_tile_sort_u64": (_i32, [_vp, _i64, _i64, _vp]),

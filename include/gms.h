@@ -86,6 +86,29 @@ int gms_sort_kv_f64_i32(double* keys_in, int32_t* vals_in, double* keys_out, int
                         int thread_blocks, void* stream);
 
 /* ---------------------------------------------------------------------------
+ * Allocation-free int32 sort.  No counterpart in the reference (its
+ * multimergesort allocates its pivots array with cudaMalloc on every call,
+ * src/multimergesort.hxx:62-63).
+ *
+ * For callers that cannot allocate device memory while they run -- a
+ * latency-critical serving loop, where cudaMalloc/cudaFree can synchronize the
+ * device and stall other streams, or a host framework that fixes each plugin's
+ * memory at start-up and forbids allocation in its callbacks.  Same contract
+ * as gms_sort_i32 (result in `output`, `input` clobbered), but every byte of
+ * scratch lives in one static 4 MiB device array of the library, held by each
+ * GPU that loads it until the process exits.  Limits and rules:
+ *   - n <= GMS_NOALLOC_MAX_N, else GMS_ERR_TOO_LARGE; always the default
+ *     tuning (fan-in 32, sample block 32), whatever gms_set_tune says;
+ *   - the first call on a device (with that device current) looks up the
+ *     array's device address; make it before any stream capture;
+ *   - all calls share the array: calls whose GPU work overlaps race, so order
+ *     them (one stream, or explicit events).
+ * It calls no cudaMalloc, cudaFree or other allocating routine.
+ * ------------------------------------------------------------------------- */
+#define GMS_NOALLOC_MAX_N ((int64_t)1 << 22)
+int gms_sort_i32_noalloc(int32_t* input, int32_t* output, int64_t n, void* stream);
+
+/* ---------------------------------------------------------------------------
  * End-to-end sorts from host memory: copy n keys from `host_in` to the device,
  * sort, copy the result to `host_out` (may equal host_in), and wait for the
  * stream.  Device buffers come from the library's per-stream cache (allocated
