@@ -206,21 +206,25 @@ __device__ __forceinline__ void sts(uint32_t addr, const T& x) {
   }
 }
 
-// Loaders.  PlainLoad reads keys as stored; EncLoad applies the codec (used
-// when a merge reads raw user keys straight from a staging buffer).
+// Loaders.  Keys are addressed by 32-bit shared-window BYTE addresses, so a
+// merge step advances a pointer by sizeof(KeyT) and loads at an immediate
+// offset, with no index multiply.  PlainLoad reads keys as stored; EncLoad
+// applies the codec (a merge reading raw user keys from a staging buffer).
 template <class KeyT>
 struct PlainLoad {
   uint32_t base;  // shared-window byte address of element 0
   __device__ __forceinline__ explicit PlainLoad(const KeyT* p) : base(static_cast<uint32_t>(__cvta_generic_to_shared(p))) {}
-  __device__ __forceinline__ KeyT operator()(int i) const { return lds<KeyT>(base + (uint32_t)i * (uint32_t)sizeof(KeyT)); }
+  __device__ __forceinline__ uint32_t addr(int i) const { return base + (uint32_t)i * (uint32_t)sizeof(KeyT); }
+  __device__ __forceinline__ KeyT at(uint32_t a) const { return lds<KeyT>(a); }
 };
 template <class KeyT, class Codec>
 struct EncLoad {
   uint32_t base;
   int on;
   __device__ __forceinline__ EncLoad(const KeyT* p, int on_) : base(static_cast<uint32_t>(__cvta_generic_to_shared(p))), on(on_) {}
-  __device__ __forceinline__ KeyT operator()(int i) const {
-    const KeyT x = lds<KeyT>(base + (uint32_t)i * (uint32_t)sizeof(KeyT));
+  __device__ __forceinline__ uint32_t addr(int i) const { return base + (uint32_t)i * (uint32_t)sizeof(KeyT); }
+  __device__ __forceinline__ KeyT at(uint32_t a) const {
+    const KeyT x = lds<KeyT>(a);
     return on ? Codec::enc(x) : x;
   }
 };
@@ -234,57 +238,61 @@ struct SmemArray {
   __device__ __forceinline__ T get(int i) const { return lds<T>(base + (uint32_t)i * (uint32_t)sizeof(T)); }
 };
 
-// Merge path over [lo, hi]: number of elements of A = [a0, a0+na) among the
-// first `diag` outputs of the stable merge of A and B = [b0, b0+nb) (A wins
-// ties), searched only inside [lo, hi].  Branch-free steps.
-template <class Ld, class Cmp>
-__device__ __forceinline__ int merge_path_in(const Ld& ld, int a0, int b0, int diag, int lo, int hi, Cmp cmp) {
+// Merge path over [lo, hi]: number of elements of A (byte address a0) among the
+// first `diag` outputs of the stable merge of A and B (byte address b0), A
+// winning ties, searched only inside [lo, hi].  Branch-free steps.
+template <class KeyT, class Ld, class Cmp>
+__device__ __forceinline__ int merge_path_in(const Ld& ld, uint32_t a0, uint32_t b0, int diag, int lo, int hi,
+                                             Cmp cmp) {
+  constexpr uint32_t S = sizeof(KeyT);
+  const uint32_t bd = b0 + (uint32_t)(diag - 1) * S;  // B[diag-1-mid] = bd - mid*S
   int len = hi - lo;
   while (len > 0) {
     const int half = len >> 1;
     const int mid = lo + half;
-    const bool go = !cmp(ld(b0 + diag - 1 - mid), ld(a0 + mid));
+    const bool go = !cmp(ld.at(bd - (uint32_t)mid * S), ld.at(a0 + (uint32_t)mid * S));
     lo = go ? mid + 1 : lo;
     len = go ? len - half - 1 : half;
   }
   return lo;
 }
 
-template <class Ld, class Cmp>
-__device__ __forceinline__ int merge_path(const Ld& ld, int a0, int na, int b0, int nb, int diag, Cmp cmp) {
+template <class KeyT, class Ld, class Cmp>
+__device__ __forceinline__ int merge_path(const Ld& ld, uint32_t a0, int na, uint32_t b0, int nb, int diag, Cmp cmp) {
   const int lo = diag - nb > 0 ? diag - nb : 0;
   const int hi = diag < na ? diag : na;
-  return merge_path_in(ld, a0, b0, diag, lo, hi, cmp);
+  return merge_path_in<KeyT>(ld, a0, b0, diag, lo, hi, cmp);
 }
 
-// Cursor of a stable two-way merge.  A = [xa, ea), B = [xb, eb) (absolute
-// indices of one buffer); ka/kb are the heads.  step() emits the smaller head
-// (A wins ties) and advances that side with one unconditional load at the
-// consumed index + 1 (buffers carry slack elements, so this stays in bounds).
-// No branches.
+// Cursor of a stable two-way merge.  A = [xa, ea), B = [xb, eb) as byte
+// addresses; ka/kb are the heads.  step() emits the smaller head (A wins ties)
+// and advances that side with one unconditional load right after the consumed
+// element (buffers carry slack elements, so it stays in bounds).  No branches.
 template <class KeyT>
 struct MergeCursor {
-  int xa, ea, xb, eb;
+  uint32_t xa, ea, xb, eb;
   KeyT ka, kb;
 
   template <class Ld>
-  __device__ __forceinline__ void init(const Ld& ld, int a0, int a1, int b0, int b1) {
+  __device__ __forceinline__ void init(const Ld& ld, uint32_t a0, uint32_t a1, uint32_t b0, uint32_t b1) {
     xa = a0;
     ea = a1;
     xb = b0;
     eb = b1;
-    ka = ld(a0);
-    kb = ld(b0);
+    ka = ld.at(a0);
+    kb = ld.at(b0);
   }
 
+  // Returns the emitted key; `src` receives its byte address, `took_a` its side.
   template <class Ld, class Cmp>
-  __device__ __forceinline__ KeyT step(const Ld& ld, Cmp cmp, int& src, bool& took_a) {
+  __device__ __forceinline__ KeyT step(const Ld& ld, Cmp cmp, uint32_t& src, bool& took_a) {
+    constexpr uint32_t S = sizeof(KeyT);
     const bool ta = (xb >= eb) || ((xa < ea) && !cmp(kb, ka));
     const KeyT o = ta ? ka : kb;
-    const int cur = ta ? xa : xb;
-    const KeyT nv = ld(cur + 1);
-    xa = ta ? cur + 1 : xa;
-    xb = ta ? xb : cur + 1;
+    const uint32_t cur = ta ? xa : xb;
+    const KeyT nv = ld.at(cur + S);
+    xa = ta ? cur + S : xa;
+    xb = ta ? xb : cur + S;
     ka = ta ? nv : ka;
     kb = ta ? kb : nv;
     src = cur;
@@ -295,17 +303,18 @@ struct MergeCursor {
   __device__ __forceinline__ bool exhausted() const { return xa + xb == ea + eb; }
 };
 
-// One merge pair of a level: its first output position and its two runs.
+// One merge pair of a level: its first output position and its two runs
+// (element indices into the level's input buffer).
 struct PairRange {
   int out0;    // output position of the pair's first element
-  int a0, ea;  // run A (absolute buffer indices)
+  int a0, ea;  // run A
   int b0, eb;  // run B
   int id;      // pair index (for payload lookups)
 };
 
 // Produces the ITEMS outputs [s, s+ITEMS) of one merge level.
-//   pair_of(q)          -> PairRange of the pair holding output position q
-//   emit(i, key, src, ta, pair) stores output i
+//   pair_of(q)  -> PairRange of the pair holding output position q
+//   emit(i, key, src_index, took_a, pair) stores output i
 // When all ITEMS outputs lie in one pair (the common case) the thread runs two
 // independent merge streams (outputs [s, s+H) and [s+H, s+ITEMS)), so two
 // dependency chains are in flight; the second stream's merge-path search only
@@ -315,28 +324,31 @@ struct PairRange {
 template <int ITEMS, class KeyT, class Ld, class Cmp, class PairOf, class Emit>
 __device__ __forceinline__ void merge_thread(int s, const Ld& ld, Cmp cmp, const PairOf& pair_of, const Emit& emit) {
   constexpr int H = (ITEMS + 1) / 2;
+  constexpr uint32_t S = sizeof(KeyT);
   PairRange P = pair_of(s);
   const int na = P.ea - P.a0, nb = P.eb - P.b0;
   const int diag = s - P.out0;
+  uint32_t A0 = ld.addr(P.a0), B0 = ld.addr(P.b0);
   if (na + nb - diag >= ITEMS) {
-    const int ia1 = merge_path(ld, P.a0, na, P.b0, nb, diag, cmp);
+    const int ia1 = merge_path<KeyT>(ld, A0, na, B0, nb, diag, cmp);
     const int d2 = diag + H;
     int lo2 = d2 - nb > ia1 ? d2 - nb : ia1;
     int hi2 = ia1 + H;
     hi2 = hi2 < na ? hi2 : na;
     hi2 = hi2 < d2 ? hi2 : d2;
-    const int ia2 = merge_path_in(ld, P.a0, P.b0, d2, lo2, hi2, cmp);
+    const int ia2 = merge_path_in<KeyT>(ld, A0, B0, d2, lo2, hi2, cmp);
+    const uint32_t EA = A0 + (uint32_t)na * S, EB = B0 + (uint32_t)nb * S;
     MergeCursor<KeyT> c1, c2;
-    c1.init(ld, P.a0 + ia1, P.ea, P.b0 + (diag - ia1), P.eb);
-    c2.init(ld, P.a0 + ia2, P.ea, P.b0 + (d2 - ia2), P.eb);
+    c1.init(ld, A0 + (uint32_t)ia1 * S, EA, B0 + (uint32_t)(diag - ia1) * S, EB);
+    c2.init(ld, A0 + (uint32_t)ia2 * S, EA, B0 + (uint32_t)(d2 - ia2) * S, EB);
 #pragma unroll
     for (int i = 0; i < H; ++i) {
-      int src1;
+      uint32_t src1;
       bool ta1;
       const KeyT o1 = c1.step(ld, cmp, src1, ta1);
       emit(i, o1, src1, ta1, P);
       if (H + i < ITEMS) {
-        int src2;
+        uint32_t src2;
         bool ta2;
         const KeyT o2 = c2.step(ld, cmp, src2, ta2);
         emit(H + i, o2, src2, ta2, P);
@@ -344,16 +356,18 @@ __device__ __forceinline__ void merge_thread(int s, const Ld& ld, Cmp cmp, const
     }
     return;
   }
-  const int ia = merge_path(ld, P.a0, na, P.b0, nb, diag, cmp);
+  const int ia = merge_path<KeyT>(ld, A0, na, B0, nb, diag, cmp);
   MergeCursor<KeyT> c;
-  c.init(ld, P.a0 + ia, P.ea, P.b0 + (diag - ia), P.eb);
+  c.init(ld, A0 + (uint32_t)ia * S, A0 + (uint32_t)na * S, B0 + (uint32_t)(diag - ia) * S, B0 + (uint32_t)nb * S);
 #pragma unroll
   for (int i = 0; i < ITEMS; ++i) {
     if (c.exhausted()) {
       P = pair_of(s + i);
-      c.init(ld, P.a0, P.ea, P.b0, P.eb);
+      A0 = ld.addr(P.a0);
+      B0 = ld.addr(P.b0);
+      c.init(ld, A0, ld.addr(P.ea), B0, ld.addr(P.eb));
     }
-    int src;
+    uint32_t src;
     bool ta;
     const KeyT o = c.step(ld, cmp, src, ta);
     emit(i, o, src, ta, P);

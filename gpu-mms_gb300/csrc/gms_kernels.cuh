@@ -211,9 +211,9 @@ __global__ void __launch_bounds__(NT, (MODE == MODE_BASE && sizeof(KeyT) == 4 &&
       const SmemArray<KeyT> yka(yk + s);
       const SmemArray<V> xva(xv), yva(yv + s);
       const RegularPairs pairs{rl, CAP};
-      merge_thread<ITEMS, KeyT>(s, ld, cmp, pairs, [&](int i, KeyT k, int src, bool, const PairRange&) {
+      merge_thread<ITEMS, KeyT>(s, ld, cmp, pairs, [&](int i, KeyT k, uint32_t src, bool, const PairRange&) {
         yka.put(i, k);
-        if constexpr (kHasVal) yva.put(i, xva.get(src));
+        if constexpr (kHasVal) yva.put(i, xva.get((int)((src - ld.base) / (uint32_t)sizeof(KeyT))));
       });
       __syncthreads();
       cur ^= 1;
@@ -303,10 +303,10 @@ __global__ void __launch_bounds__(NT, (MODE == MODE_BASE && sizeof(KeyT) == 4 &&
         const PlainLoad<KeyT> ld(xk);
         const SmemArray<KeyT> yka(yk + s);
         const SmemArray<V> xva(xv), yva(yv + s);
-        const CompactPairs pairs{pre, nk, span, (nk + span - 1) / span};
-        merge_thread<ITEMS, KeyT>(s, ld, cmp, pairs, [&](int i, KeyT k, int src, bool, const PairRange&) {
+        const CompactPairs pairs{pre, nk, span, (nk + span - 1) >> (31 - __clz(span))};
+        merge_thread<ITEMS, KeyT>(s, ld, cmp, pairs, [&](int i, KeyT k, uint32_t src, bool, const PairRange&) {
           yka.put(i, k);
-          if constexpr (kHasVal) yva.put(i, xva.get(src));
+          if constexpr (kHasVal) yva.put(i, xva.get((int)((src - ld.base) / (uint32_t)sizeof(KeyT))));
         });
       }
       __syncthreads();
@@ -517,13 +517,21 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
   }
 
   // ---- wait for the staged segments (bounded) ----
+  // Only warp 0 polls the mbarrier; the other warps wait in the block barrier,
+  // which issues nothing.  The barrier orders warp 0's acquire of the copied
+  // bytes (and its own plain stores) before every other thread's reads.
   constexpr uint32_t kSpinLimit = 1u << 26;
-  if (!mbar_wait_bounded(bar, 0, kSpinLimit)) {
-    if (tid == 0 && a.err) atomicOr(a.err, DEV_COPY_TIMEOUT);
-    mbar_wait_bounded(bar, 0, kSpinLimit);  // let copies in flight land
-    return;
+  int* timed_out = cpre + 97;  // the padding word after the descriptors
+  if (tid < 32) {
+    const bool ok = mbar_wait_bounded(bar, 0, kSpinLimit);
+    if (lane == 0) *timed_out = ok ? 0 : 1;
+    if (!ok) {
+      if (lane == 0 && a.err) atomicOr(a.err, DEV_COPY_TIMEOUT);
+      mbar_wait_bounded(bar, 0, kSpinLimit);  // let copies in flight land
+    }
   }
-  __syncthreads();  // plain-loaded bytes from warp 0 are visible
+  __syncthreads();
+  if (*timed_out) return;
   const int cnt = (int)meta[3];
   if (cnt < 0) return;  // rejected tile (never expected): nothing was copied
   const int64_t out_base = meta[0];
@@ -549,11 +557,11 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
     const SmemArray<V> yva(v1 + s);
     const SmemArray<V> sva(reinterpret_cast<const V*>(stage_v));
     const int gen = a.gen_index;
-    merge_thread<ITEMS, KeyT>(s, ld, cmp, pair_of, [&](int i, KeyT k, int src, bool ta, const PairRange& P) {
+    merge_thread<ITEMS, KeyT>(s, ld, cmp, pair_of, [&](int i, KeyT k, uint32_t src, bool ta, const PairRange& P) {
       yka.put(i, k);
       if constexpr (kHasVal) {
         const int seg = ta ? 2 * P.id : 2 * P.id + 1;
-        const int off = src - sbk[seg];
+        const int off = (int)((src - ld.base) / (uint32_t)sizeof(KeyT)) - sbk[seg];
         yva.put(i, gen ? (V)(gsrc[seg] + off) : sva.get(sbv[seg] + off));
       }
     });
@@ -570,10 +578,10 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
       const PlainLoad<KeyT> ld(xk);
       const SmemArray<KeyT> yka(yk + s);
       const SmemArray<V> xva(xv), yva(yv + s);
-      const CompactPairs pairs{cpre, nk, span, (nk + span - 1) / span};
-      merge_thread<ITEMS, KeyT>(s, ld, cmp, pairs, [&](int i, KeyT k, int src, bool, const PairRange&) {
+      const CompactPairs pairs{cpre, nk, span, (nk + span - 1) >> (31 - __clz(span))};
+      merge_thread<ITEMS, KeyT>(s, ld, cmp, pairs, [&](int i, KeyT k, uint32_t src, bool, const PairRange&) {
         yka.put(i, k);
-        if constexpr (kHasVal) yva.put(i, xva.get(src));
+        if constexpr (kHasVal) yva.put(i, xva.get((int)((src - ld.base) / (uint32_t)sizeof(KeyT))));
       });
     }
     __syncthreads();

@@ -186,9 +186,12 @@ inline cudaError_t ensure_smem(const void* kern, size_t bytes) {
 //   Cmp    strict weak order on K
 //   Codec  user bits <-> K
 //   STABLE stable base case (key/value sorts, user comparators)
-template <class KeyT, class V, class Cmp, class Codec, bool STABLE, int NT, int ITEMS>
+template <class KeyT, class V, class Cmp, class Codec, bool STABLE, int NT, int ITEMS, int NTM = NT,
+          int ITEMSM = ITEMS>
 struct Engine {
+  // base-case tile (NT threads x ITEMS keys) and merge tile (NTM x ITEMSM)
   static constexpr int CAP = NT * ITEMS;
+  static constexpr int CAPM = NTM * ITEMSM;
   using IdxT = uint32_t;
 
   // ---------------- geometry ----------------
@@ -201,13 +204,13 @@ struct Engine {
   // Walks the recursion of one merge round and records scratch sizes.
   static void plan_round(WsLayout& l, int level, int64_t n, int64_t L, const Tune& t, bool gather0 = false) {
     const int k = t.k;
-    if ((int64_t)k * L <= CAP) return;  // GROUP mode, no scratch
+    if ((int64_t)k * L <= CAPM) return;  // GROUP mode, no scratch
     if (level + 1 >= kMaxLevels) {
       l.ok = false;  // sample recursion too deep for this tuning
       return;
     }
     const int sb = t.sample_b;
-    const int64_t G = CAP / sb - k;
+    const int64_t G = CAPM / sb - k;
     const int64_t runs = ceil_div(n, L);
     const int64_t Ls = ceil_div(L, sb);
     const int64_t ns = (runs - 1) * Ls + ceil_div(n - (runs - 1) * L, sb);
@@ -246,14 +249,16 @@ struct Engine {
   static cudaError_t launch_tile(const TileArgs<KeyT, VV>& a, int64_t grid, cudaStream_t st, int level = 0) {
     if (grid <= 0) return cudaSuccess;
     constexpr bool kStable = (MODE == MODE_BASE) ? STABLE : false;
-    auto kern = tile_kernel<KeyT, VV, Cmp, Codec, MODE, kStable, NT, ITEMS>;
-    const size_t smem = TileSmemLayout<KeyT, VV, CAP>::bytes;
+    constexpr int kNT = (MODE == MODE_BASE) ? NT : NTM;
+    constexpr int kIT = (MODE == MODE_BASE) ? ITEMS : ITEMSM;
+    auto kern = tile_kernel<KeyT, VV, Cmp, Codec, MODE, kStable, kNT, kIT>;
+    const size_t smem = TileSmemLayout<KeyT, VV, kNT * kIT>::bytes;
     cudaError_t e = ensure_smem((const void*)kern, smem);
     if (e != cudaSuccess) return e;
     if (grid > 0x7fffffff) return cudaErrorInvalidConfiguration;
     const int kc = (MODE == MODE_BASE) ? KC_BASE : (level == 0 ? KC_MERGE : KC_SAMPLE_MERGE);
     hook_before(kc, st);
-    kern<<<(unsigned)grid, NT, smem, st>>>(a);
+    kern<<<(unsigned)grid, kNT, smem, st>>>(a);
     e = cudaGetLastError();
     hook_after(kc, st);
     return e;
@@ -265,13 +270,13 @@ struct Engine {
                                         int level) {
     if (total_tiles <= 0) return cudaSuccess;
     if (total_tiles > 0x7fffffff) return cudaErrorInvalidConfiguration;
-    auto kern = merge_tiles_kernel<KeyT, VV, Cmp, Codec, NT, ITEMS>;
-    const size_t smem = MergeSmemLayout<KeyT, VV, CAP>::bytes;
+    auto kern = merge_tiles_kernel<KeyT, VV, Cmp, Codec, NTM, ITEMSM>;
+    const size_t smem = MergeSmemLayout<KeyT, VV, CAPM>::bytes;
     cudaError_t e = ensure_smem((const void*)kern, smem);
     if (e != cudaSuccess) return e;
     const int kc = level == 0 ? KC_MERGE : KC_SAMPLE_MERGE;
     hook_before(kc, st);
-    kern<<<(unsigned)total_tiles, NT, smem, st>>>(a, total_tiles);
+    kern<<<(unsigned)total_tiles, NTM, smem, st>>>(a, total_tiles);
     e = cudaGetLastError();
     hook_after(kc, st);
     return e;
@@ -303,11 +308,11 @@ struct Engine {
     a.out_run_len = L * k;
     a.sample_run_len = ceil_div(L * k, sb);
     const int64_t groups = ceil_div(n, L * k);
-    if ((int64_t)k * L <= CAP) {
+    if ((int64_t)k * L <= CAPM) {
       return launch_tile<MODE_GROUP>(a, groups, st, level);
     }
     if (level + 1 >= kMaxLevels) return cudaErrorInvalidValue;
-    const int64_t G = CAP / sb - k;
+    const int64_t G = CAPM / sb - k;
     const int64_t runs = ceil_div(n, L);
     const int64_t Ls = ceil_div(L, sb);
     const int64_t ns = (runs - 1) * Ls + ceil_div(n - (runs - 1) * L, sb);
