@@ -230,16 +230,14 @@ int gms_timing_reset(void) {
 int64_t gms_max_tile(void) { return (int64_t)kNT * kItems; }
 
 int64_t gms_base_tile(int dtype, int kv) {
-  (void)dtype;
-  (void)kv;
-  return (int64_t)kNT * kItems;
+  if (kv) return KvEngine<uint32_t, gms::IdentityCodec<uint32_t>>::BASE_TILE;
+  if (dtype >= 3) return KeysEngine<uint64_t, gms::IdentityCodec<uint64_t>>::BASE_TILE;
+  return KeysEngine<uint32_t, gms::IdentityCodec<uint32_t>>::BASE_TILE;
 }
 
 int gms_rounds(int dtype, int kv, int64_t n) {
-  (void)dtype;
-  (void)kv;
   int p = 0;
-  for (int64_t L = (int64_t)kNT * kItems; L < n; L *= default_tune().k) ++p;
+  for (int64_t L = gms_base_tile(dtype, kv); L < n; L *= default_tune().k) ++p;
   return p;
 }
 

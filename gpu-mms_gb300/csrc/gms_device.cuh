@@ -164,6 +164,60 @@ __device__ __forceinline__ void transposition_sort(KeyT (&r)[N], V (&v)[N], Cmp 
 }
 
 // ---------------------------------------------------------------------------
+// Warp-wide bitonic merging of per-lane sorted runs (keys-only, unstable).
+//
+// Reference counterpart: merge32..merge512 / merge*dir with __shfl_xor_sync
+// (GPU-MMS src/basecase/sortRowMajor.hxx:133-311).  Here each lane holds KPL
+// keys sorted ascending in registers, the warp's element e = lane*KPL + r
+// (row-major), and five phases merge lane runs into one sorted run of 32*KPL
+// keys: phase q merges pairs of runs spread over 2^(q-1) lanes by a mirror
+// ("flip") exchange followed by half-cleaners -- across lanes for strides of
+// at least KPL elements, inside the lane for smaller ones.  The partner of a
+// mirror exchange is register KPL-1-r of lane ^ (2^q - 1); registers r and
+// KPL-1-r are exchanged together so only two temporaries are live.
+template <class KeyT, class Cmp>
+__device__ __forceinline__ KeyT keep_lo_hi(bool lo, const KeyT& a, const KeyT& b, Cmp cmp) {
+  const bool blt = cmp(b, a);
+  return lo ? (blt ? b : a) : (blt ? a : b);
+}
+
+template <int KPL, class KeyT, class Cmp>
+__device__ __forceinline__ void warp_merge_runs(KeyT (&x)[KPL], Cmp cmp) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int q = 1; q <= 5; ++q) {
+    const int G = 1 << q;
+    const bool lower = (lane & (G >> 1)) == 0;
+    // mirror exchange with lane ^ (G-1), register KPL-1-r
+#pragma unroll
+    for (int r = 0; r < KPL / 2; ++r) {
+      const KeyT ya = __shfl_xor_sync(0xffffffffu, x[KPL - 1 - r], G - 1);
+      const KeyT yb = __shfl_xor_sync(0xffffffffu, x[r], G - 1);
+      x[r] = keep_lo_hi(lower, x[r], ya, cmp);
+      x[KPL - 1 - r] = keep_lo_hi(lower, x[KPL - 1 - r], yb, cmp);
+    }
+    // half-cleaners across lanes (element strides 16*G/4 ... KPL)
+#pragma unroll
+    for (int m = G >> 2; m >= 1; m >>= 1) {
+      const bool lo = (lane & m) == 0;
+#pragma unroll
+      for (int r = 0; r < KPL; ++r) {
+        const KeyT z = __shfl_xor_sync(0xffffffffu, x[r], m);
+        x[r] = keep_lo_hi(lo, x[r], z, cmp);
+      }
+    }
+    // half-cleaners inside the lane (strides KPL/2 ... 1)
+#pragma unroll
+    for (int sd = KPL / 2; sd >= 1; sd >>= 1) {
+#pragma unroll
+      for (int r = 0; r < KPL; ++r) {
+        if ((r & sd) == 0) cas(x[r], x[r + sd], cmp);
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Shared-memory access through 32-bit shared-window addresses.  For 4- and
 // 8-byte keys the loads are explicit ld.shared (no generic 64-bit address
 // arithmetic); other types use ordinary accesses.

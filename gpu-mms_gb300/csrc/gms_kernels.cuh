@@ -332,6 +332,105 @@ __global__ void __launch_bounds__(NT, (MODE == MODE_BASE && sizeof(KeyT) == 4 &&
 }
 
 // ---------------------------------------------------------------------------
+// Base case for keys-only sorts of 4- and 8-byte keys: register network per
+// lane, warp-shuffle bitonic merges up to one 32*KPL-key run per warp, then
+// shared-memory merge-path levels up to the TILE = NT*KPL-key tile.
+//
+// Reference counterpart: squareSort (GPU-MMS src/basecase/squareSort.hxx:62-131)
+// with its register sort (bitonicSort32) and shuffle merges (merge32..512).
+template <int NT, int KPL, int ITEMS_M>
+struct BaseWarpGeom {
+  static constexpr int TILE = NT * KPL;
+  static constexpr int WARP_RUN = 32 * KPL;
+  static constexpr int MERGE_THREADS = (TILE + ITEMS_M - 1) / ITEMS_M;
+  static_assert(MERGE_THREADS <= NT, "merge phase needs TILE <= NT*ITEMS_M");
+  static_assert((KPL & (KPL - 1)) == 0 && KPL % 4 == 0, "KPL must be a power of two, multiple of 4");
+};
+
+// Each ping-pong buffer covers every position a merge thread emits
+// (MERGE_THREADS*ITEMS_M, which can exceed TILE) plus slack for the cursor's
+// look-past load.
+template <class KeyT, int NT, int KPL, int ITEMS_M>
+struct BaseWarpSmem {
+  using Geo = BaseWarpGeom<NT, KPL, ITEMS_M>;
+  static constexpr int SPAN = Geo::MERGE_THREADS * ITEMS_M > Geo::TILE ? Geo::MERGE_THREADS * ITEMS_M : Geo::TILE;
+  static constexpr size_t buf = ((sizeof(KeyT) * (SPAN + 4) + 15) / 16) * 16;
+  static constexpr size_t bytes = 2 * buf;
+};
+
+template <class KeyT, class Cmp, class Codec, int NT, int KPL, int ITEMS_M>
+__global__ void __launch_bounds__(NT) base_warp_kernel(TileArgs<KeyT, NoVal> a) {
+  using Geo = BaseWarpGeom<NT, KPL, ITEMS_M>;
+  constexpr int TILE = Geo::TILE;
+  constexpr size_t BUF = BaseWarpSmem<KeyT, NT, KPL, ITEMS_M>::buf;
+  extern __shared__ __align__(16) unsigned char smem[];
+  KeyT* const k0 = reinterpret_cast<KeyT*>(smem);
+  KeyT* const k1 = reinterpret_cast<KeyT*>(smem + BUF);
+  const Cmp cmp;
+  const int tid = threadIdx.x;
+  const int lane = tid & 31;
+  const int warp = tid >> 5;
+  const int64_t base = (int64_t)blockIdx.x * TILE;
+  if (base >= a.n) return;
+  const int cnt = (int)min64(TILE, a.n - base);
+
+  // Coalesced striped load: register i of thread t holds element t + i*NT.
+  KeyT x[KPL];
+#pragma unroll
+  for (int i = 0; i < KPL; ++i) {
+    const int p = tid + i * NT;
+    if (p < cnt) x[i] = maybe_enc<Codec>(a.in[base + p], a.enc_on_load);
+  }
+  if (cnt < TILE) {
+    // a short last tile is padded with copies of its largest key
+    KeyT m = x[0];
+    if (tid >= cnt) m = maybe_enc<Codec>(a.in[base], a.enc_on_load);
+#pragma unroll
+    for (int i = 1; i < KPL; ++i) {
+      if (tid + i * NT < cnt) m = cmp(m, x[i]) ? x[i] : m;
+    }
+    m = block_max<NT>(m, k0, cmp);
+#pragma unroll
+    for (int i = 0; i < KPL; ++i) {
+      if (tid + i * NT >= cnt) x[i] = m;
+    }
+  }
+  network_sort<KPL>(x, cmp);
+  warp_merge_runs<KPL>(x, cmp);
+  // The warp's sorted run: lane l holds elements l*KPL .. l*KPL+KPL-1.
+  {
+    const SmemArray<KeyT> dst(k0 + warp * Geo::WARP_RUN + lane * KPL);
+#pragma unroll
+    for (int r = 0; r < KPL; ++r) dst.put(r, x[r]);
+  }
+  __syncthreads();
+  // shared-memory merge levels: runs of WARP_RUN ... TILE/2
+  int cur = 0;
+  const int s = tid * ITEMS_M;
+  for (int rl = Geo::WARP_RUN; rl < TILE; rl *= 2) {
+    const KeyT* xk = cur ? k1 : k0;
+    KeyT* yk = cur ? k0 : k1;
+    if (tid < Geo::MERGE_THREADS) {
+      const PlainLoad<KeyT> ld(xk);
+      const SmemArray<KeyT> yka(yk + s);
+      const RegularPairs pairs{rl, TILE};
+      merge_thread<ITEMS_M, KeyT>(s, ld, cmp, pairs,
+                                  [&](int i, KeyT k, uint32_t, bool, const PairRange&) { yka.put(i, k); });
+    }
+    __syncthreads();
+    cur ^= 1;
+  }
+  // coalesced store (+ block sample of the output run = this tile)
+  const KeyT* fk = cur ? k1 : k0;
+  for (int p = tid; p < cnt; p += NT) a.out[base + p] = maybe_dec<Codec>(fk[p], a.dec_on_store);
+  if (a.sample_out) {
+    for (int p = tid * a.sample_b; p < cnt; p += NT * a.sample_b) {
+      a.sample_out[(int64_t)blockIdx.x * a.sample_run_len + p / a.sample_b] = fk[p];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // K-way merge of one forecast tile per CTA, staged with bulk copies.
 //
 // Warp 0 places the K run segments of the tile in the staging buffer

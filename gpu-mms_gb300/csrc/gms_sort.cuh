@@ -24,6 +24,7 @@
 #include <cstdint>
 #include <cstring>
 #include <mutex>
+#include <type_traits>
 
 #include "gms_kernels.cuh"
 
@@ -192,12 +193,20 @@ struct Engine {
   // base-case tile (NT threads x ITEMS keys) and merge tile (NTM x ITEMSM)
   static constexpr int CAP = NT * ITEMS;
   static constexpr int CAPM = NTM * ITEMSM;
+  // Keys-only sorts of 4- and 8-byte integer keys use the warp-shuffle base
+  // case: 256 x 32 keys (4-byte) or 512 x 16 keys (8-byte), 8192-key tiles.
+  static constexpr bool kWarpBase =
+      !STABLE && !HasVal<V>::value && std::is_integral<KeyT>::value && (sizeof(KeyT) == 4 || sizeof(KeyT) == 8);
+  static constexpr int kNTB = sizeof(KeyT) == 4 ? 256 : 512;
+  static constexpr int kKPL = sizeof(KeyT) == 4 ? 32 : 16;
+  static constexpr int kITB = sizeof(KeyT) == 4 ? 33 : 17;
+  static constexpr int BASE_TILE = kWarpBase ? kNTB * kKPL : CAP;
   using IdxT = uint32_t;
 
   // ---------------- geometry ----------------
   static int passes_for(int64_t n, int k) {
     int p = 0;
-    for (int64_t L = CAP; L < n; L *= k) ++p;
+    for (int64_t L = BASE_TILE; L < n; L *= k) ++p;
     return p;
   }
 
@@ -230,7 +239,7 @@ struct Engine {
 
   static WsLayout plan(int64_t n, const Tune& t) {
     WsLayout l;
-    int64_t L = CAP;
+    int64_t L = BASE_TILE;
     while (L < n) {
       plan_round(l, 0, n, L, t);
       L *= t.k;
@@ -262,6 +271,28 @@ struct Engine {
     e = cudaGetLastError();
     hook_after(kc, st);
     return e;
+  }
+
+  // Warp-shuffle base case (keys-only 4/8-byte keys).
+  static cudaError_t launch_base_warp(const TileArgs<KeyT, V>& a, int64_t grid, cudaStream_t st) {
+    if constexpr (kWarpBase) {
+      if (grid <= 0) return cudaSuccess;
+      if (grid > 0x7fffffff) return cudaErrorInvalidConfiguration;
+      auto kern = base_warp_kernel<KeyT, Cmp, Codec, kNTB, kKPL, kITB>;
+      const size_t smem = BaseWarpSmem<KeyT, kNTB, kKPL, kITB>::bytes;
+      cudaError_t e = ensure_smem((const void*)kern, smem);
+      if (e != cudaSuccess) return e;
+      hook_before(KC_BASE, st);
+      kern<<<(unsigned)grid, kNTB, smem, st>>>(a);
+      e = cudaGetLastError();
+      hook_after(KC_BASE, st);
+      return e;
+    } else {
+      (void)a;
+      (void)grid;
+      (void)st;
+      return cudaErrorNotSupported;
+    }
   }
 
   // Bulk-copy merge of the forecast tiles of one round (one CTA per tile).
@@ -374,21 +405,26 @@ struct Engine {
       a.vin = vin;
       a.vout = vbuf[cur];
       a.n = n;
-      a.L = CAP;
+      a.L = BASE_TILE;
       a.k = 1;
       a.enc_on_load = 1;
       a.dec_on_store = (P == 0) ? 1 : 0;
       a.gen_index = 0;
       a.err = w.err;
       a.sample_b = t.sample_b;
-      a.out_run_len = CAP;
-      a.sample_run_len = ceil_div(CAP, t.sample_b);
+      a.out_run_len = BASE_TILE;
+      a.sample_run_len = ceil_div(BASE_TILE, t.sample_b);
       a.sample_out = (P > 0) ? w.s1[0] : nullptr;
-      cudaError_t e = launch_tile<MODE_BASE>(a, ceil_div(n, CAP), st);
+      cudaError_t e;
+      if constexpr (kWarpBase) {
+        e = launch_base_warp(a, ceil_div(n, BASE_TILE), st);
+      } else {
+        e = launch_tile<MODE_BASE>(a, ceil_div(n, CAP), st);
+      }
       if (e != cudaSuccess) return e;
     }
     int sbuf = 0;
-    int64_t L = CAP;
+    int64_t L = BASE_TILE;
     for (int p = 0; p < P; ++p) {
       const bool last = (p == P - 1);
       KeyT* sout = last ? nullptr : w.s1[sbuf ^ 1];

@@ -15,8 +15,11 @@ def ceil_div(a, b):
 
 
 class Geometry:
-    def __init__(self, cap, k, b):
+    """cap: merge-tile capacity; base: base-case tile (defaults to cap)."""
+
+    def __init__(self, cap, k, b, base=None):
         self.cap, self.k, self.b = cap, k, b
+        self.base = base or cap
         self.g = cap // b - k
         assert self.g > 0, "tile geometry needs CAP/B > K"
 
@@ -128,10 +131,10 @@ def model_sort(keys, geo):
     idx = np.arange(n, dtype=np.int64)
     stats = {}
     k = keys.copy()
-    for tb in range(0, n, geo.cap):
-        te = min(n, tb + geo.cap)
+    for tb in range(0, n, geo.base):
+        te = min(n, tb + geo.base)
         k[tb:te], idx[tb:te] = _stable_merge(k[tb:te], idx[tb:te])
-    L = geo.cap
+    L = geo.base
     rounds = 0
     while L < n:
         k, idx = model_round(k, idx, L, geo, stats)

@@ -30,9 +30,23 @@ def test_tiles_fit_and_sort_is_stable(cap, k, b):
                 assert m <= cap
 
 
-def test_production_geometry_one_round():
-    geo = Geometry(8704, 32, 32)
+@pytest.mark.parametrize("base", [8704, 8192])
+def test_production_geometry_one_round(base):
+    """Merge tiles of 8704 keys; base tiles of 8704 (key/value) or 8192
+    (keys-only warp base case)."""
+    geo = Geometry(8704, 32, 32, base=base)
     rng = np.random.default_rng(0)
-    for name, x in dists(rng, 8704 * 32 + 4321):
+    for name, x in dists(rng, base * 32 + 4321):
         sk, si, st = model_sort(x.astype(np.int64), geo)
         assert np.array_equal(si, np.argsort(x, kind="stable")), name
+        for _, m in st.get("max_tile", []):
+            assert m <= 8704
+
+
+def test_base_smaller_than_merge_tile_deep():
+    geo = Geometry(96, 4, 4, base=64)
+    rng = np.random.default_rng(5)
+    for n in [65, 256, 257, 1025, 5000]:
+        for name, x in dists(rng, n):
+            sk, si, st = model_sort(x.astype(np.int64), geo)
+            assert np.array_equal(si, np.argsort(x, kind="stable")), (n, name)
