@@ -428,121 +428,83 @@ __device__ __forceinline__ void merge_thread(int s, const Ld& ld, Cmp cmp, const
   }
 }
 
-// Warp-cooperative merge of one warp's output range of a level (keys-only;
-// equal keys are bit-identical, so tie order is not observable).
+// Warp-cooperative merge of one warp's output range [pos, end) of a level
+// (keys-only; equal keys are bit-identical, so tie order is not observable).
 //
-// Per round a chain loads the next 32 keys of run A (lane i: A[ia+i]) and of
+// Per round the warp loads the next 32 keys of run A (lane i: A[ia+i]) and of
 // run B in reverse (lane i: B[ib+31-i]) -- both contiguous, so no bank
 // conflicts.  The elementwise minimum (A wins ties) is exactly the next 32
 // outputs, as a bitonic sequence; five shuffle half-cleaner stages sort it;
 // one ballot counts how many came from A.  Near run ends missing keys count as
-// +infinity through validity flags (a uniform slow path).  A warp splits its
-// range into NC chains whose rounds are interleaved, so NC independent
-// dependency chains are in flight.  One merge-path search per chain (all
-// lanes probe the same addresses: broadcast reads).
-struct WarpChain {
-  int pos, end, na, nb, ia, ib;
-  uint32_t A0, B0;
-};
-
+// +infinity through validity flags (a uniform slow path).  One merge-path
+// search per warp (all lanes probe the same addresses: broadcast reads).
 template <class KeyT, class Ld, class Cmp, class PairOf>
-__device__ __forceinline__ void chain_start(WarpChain& c, int pos, int end, const Ld& ld, const PairOf& pair_of,
-                                            Cmp cmp) {
-  c.pos = pos;
-  c.end = end;
-  if (pos >= end) return;
-  const PairRange P = pair_of(pos);
-  c.na = P.ea - P.a0;
-  c.nb = P.eb - P.b0;
-  c.A0 = ld.addr(P.a0);
-  c.B0 = ld.addr(P.b0);
-  c.ia = merge_path<KeyT>(ld, c.A0, c.na, c.B0, c.nb, pos - P.out0, cmp);
-  c.ib = (pos - P.out0) - c.ia;
-}
-
-template <class KeyT, class Ld, class Cmp, class PairOf>
-__device__ __forceinline__ void chain_round(WarpChain& c, const Ld& ld, uint32_t dst_base, const PairOf& pair_of,
-                                            Cmp cmp) {
+__device__ __forceinline__ void warp_merge_range(int pos, int end, const Ld& ld, uint32_t dst_base,
+                                                 const PairOf& pair_of, Cmp cmp) {
   constexpr uint32_t S = sizeof(KeyT);
   const int lane = threadIdx.x & 31;
-  const int rem = (c.na - c.ia) + (c.nb - c.ib);
-  int cnt = rem < 32 ? rem : 32;
-  cnt = (c.end - c.pos) < cnt ? (c.end - c.pos) : cnt;
-  KeyT x;
-  unsigned bal;
-  if (c.ia + 32 <= c.na && c.ib + 32 <= c.nb) {
-    const KeyT av = ld.at(c.A0 + (uint32_t)(c.ia + lane) * S);
-    const KeyT bv = ld.at(c.B0 + (uint32_t)(c.ib + 31 - lane) * S);
-    const bool ta = !cmp(bv, av);
-    x = ta ? av : bv;
-    bal = __ballot_sync(0xffffffffu, ta);
+  if (pos >= end) return;
+  PairRange P = pair_of(pos);
+  int na = P.ea - P.a0, nb = P.eb - P.b0;
+  uint32_t A0 = ld.addr(P.a0), B0 = ld.addr(P.b0);
+  int ia = merge_path<KeyT>(ld, A0, na, B0, nb, pos - P.out0, cmp);
+  int ib = (pos - P.out0) - ia;
+  while (pos < end) {
+    const int rem = (na - ia) + (nb - ib);
+    int cnt = rem < 32 ? rem : 32;
+    cnt = (end - pos) < cnt ? (end - pos) : cnt;
+    KeyT x;
+    unsigned bal;
+    if (ia + 32 <= na && ib + 32 <= nb) {
+      const KeyT av = ld.at(A0 + (uint32_t)(ia + lane) * S);
+      const KeyT bv = ld.at(B0 + (uint32_t)(ib + 31 - lane) * S);
+      const bool ta = !cmp(bv, av);
+      x = ta ? av : bv;
+      bal = __ballot_sync(0xffffffffu, ta);
 #pragma unroll
-    for (int m = 16; m >= 1; m >>= 1) {
-      const KeyT y = __shfl_xor_sync(0xffffffffu, x, m);
-      const bool y_lt = cmp(y, x);
-      const bool upper = (lane & m) != 0;
-      x = (upper != y_lt) ? y : x;  // lower keeps the min, upper the max
-    }
-  } else {
-    const bool va = c.ia + lane < c.na;
-    const bool vb = c.ib + 31 - lane < c.nb;
-    const KeyT av = ld.at(c.A0 + (uint32_t)(va ? c.ia + lane : 0) * S);
-    const KeyT bv = ld.at(c.B0 + (uint32_t)(vb ? c.ib + 31 - lane : 0) * S);
-    const bool ta = va && (!vb || !cmp(bv, av));
-    x = ta ? av : bv;
-    bool vx = va || vb;
-    bal = __ballot_sync(0xffffffffu, ta);
+      for (int m = 16; m >= 1; m >>= 1) {
+        const KeyT y = __shfl_xor_sync(0xffffffffu, x, m);
+        const bool y_lt = cmp(y, x);
+        const bool upper = (lane & m) != 0;
+        x = (upper != y_lt) ? y : x;  // lower keeps the min, upper the max
+      }
+    } else {
+      const bool va = ia + lane < na;
+      const bool vb = ib + 31 - lane < nb && ib + 31 - lane >= 0;
+      const KeyT av = ld.at(A0 + (uint32_t)(va ? ia + lane : 0) * S);
+      const KeyT bv = ld.at(B0 + (uint32_t)(vb ? ib + 31 - lane : 0) * S);
+      const bool ta = va && (!vb || !cmp(bv, av));
+      x = ta ? av : bv;
+      bool vx = va || vb;
+      bal = __ballot_sync(0xffffffffu, ta);
 #pragma unroll
-    for (int m = 16; m >= 1; m >>= 1) {
-      const KeyT y = __shfl_xor_sync(0xffffffffu, x, m);
-      const bool vy = __shfl_xor_sync(0xffffffffu, vx, m);
-      const bool y_lt = vy && (!vx || cmp(y, x));
-      const bool x_lt = vx && (!vy || cmp(x, y));
-      const bool upper = (lane & m) != 0;
-      const bool take_y = upper ? x_lt : y_lt;
-      x = take_y ? y : x;
-      vx = take_y ? vy : vx;
-    }
-  }
-  if (lane < cnt) sts<KeyT>(dst_base + (uint32_t)(c.pos + lane) * S, x);
-  c.pos += cnt;
-  if (cnt == 32 && cnt < rem) {
-    const int ta_n = __popc(bal);
-    c.ia += ta_n;
-    c.ib += 32 - ta_n;
-  } else if (cnt == rem && c.pos < c.end) {
-    // pair finished: continue with the pair holding `pos`
-    const PairRange P = pair_of(c.pos);
-    c.na = P.ea - P.a0;
-    c.nb = P.eb - P.b0;
-    c.A0 = ld.addr(P.a0);
-    c.B0 = ld.addr(P.b0);
-    c.ia = 0;
-    c.ib = 0;
-  }
-}
-
-template <int NC, class KeyT, class Ld, class Cmp, class PairOf>
-__device__ __forceinline__ void warp_merge_range(int wbeg, int wend, const Ld& ld, uint32_t dst_base,
-                                                 const PairOf& pair_of, Cmp cmp) {
-  if (wbeg >= wend) return;
-  const int part = (((wend - wbeg) + NC - 1) / NC + 31) & ~31;
-  WarpChain c[NC];
-#pragma unroll
-  for (int j = 0; j < NC; ++j) {
-    const int p0 = min(wend, wbeg + j * part);
-    chain_start<KeyT>(c[j], p0, min(wend, p0 + part), ld, pair_of, cmp);
-  }
-  while (true) {
-    bool any = false;
-#pragma unroll
-    for (int j = 0; j < NC; ++j) {
-      if (c[j].pos < c[j].end) {
-        any = true;
-        chain_round<KeyT>(c[j], ld, dst_base, pair_of, cmp);
+      for (int m = 16; m >= 1; m >>= 1) {
+        const KeyT y = __shfl_xor_sync(0xffffffffu, x, m);
+        const bool vy = __shfl_xor_sync(0xffffffffu, vx, m);
+        const bool y_lt = vy && (!vx || cmp(y, x));
+        const bool x_lt = vx && (!vy || cmp(x, y));
+        const bool upper = (lane & m) != 0;
+        const bool take_y = upper ? x_lt : y_lt;
+        x = take_y ? y : x;
+        vx = take_y ? vy : vx;
       }
     }
-    if (!any) break;
+    if (lane < cnt) sts<KeyT>(dst_base + (uint32_t)(pos + lane) * S, x);
+    pos += cnt;
+    if (cnt == 32 && cnt < rem) {
+      const int ta_n = __popc(bal);
+      ia += ta_n;
+      ib += 32 - ta_n;
+    } else if (cnt == rem && pos < end) {
+      // pair finished: continue with the pair holding `pos`
+      P = pair_of(pos);
+      na = P.ea - P.a0;
+      nb = P.eb - P.b0;
+      A0 = ld.addr(P.a0);
+      B0 = ld.addr(P.b0);
+      ia = 0;
+      ib = 0;
+    }
   }
 }
 

@@ -405,7 +405,7 @@ __global__ void __launch_bounds__(NT) base_warp_kernel(TileArgs<KeyT, NoVal> a) 
     KeyT* yk = cur ? k0 : k1;
     const PlainLoad<KeyT> ld(xk);
     const RegularPairs pairs{rl, TILE};
-    warp_merge_range<4, KeyT>(warp * WR, warp * WR + WR, ld, static_cast<uint32_t>(__cvta_generic_to_shared(yk)), pairs,
+    warp_merge_range<KeyT>(warp * WR, warp * WR + WR, ld, static_cast<uint32_t>(__cvta_generic_to_shared(yk)), pairs,
                            cmp);
     __syncthreads();
     cur ^= 1;
@@ -648,7 +648,7 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
       const int b0 = (kb_ < nk) ? sbk[kb_] : a0 + na;
       return PairRange{cpre[ka_], a0, a0 + na, b0, b0 + nb, p};
     };
-    warp_merge_range<4, KeyT>(wbeg, wend, ld, static_cast<uint32_t>(__cvta_generic_to_shared(k1)), pair_of, cmp);
+    warp_merge_range<KeyT>(wbeg, wend, ld, static_cast<uint32_t>(__cvta_generic_to_shared(k1)), pair_of, cmp);
   } else if (s < cnt) {
     const int npairs = (nk + 1) / 2;
     const EncLoad<KeyT, Codec> ld(reinterpret_cast<const KeyT*>(stage_k), a.enc_on_load);
@@ -686,7 +686,7 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
     if constexpr (!kHasVal) {
       const PlainLoad<KeyT> ld(xk);
       const CompactPairs pairs{cpre, nk, span, (nk + span - 1) >> (31 - __clz(span))};
-      warp_merge_range<4, KeyT>(wbeg, wend, ld, static_cast<uint32_t>(__cvta_generic_to_shared(yk)), pairs, cmp);
+      warp_merge_range<KeyT>(wbeg, wend, ld, static_cast<uint32_t>(__cvta_generic_to_shared(yk)), pairs, cmp);
     } else if (s < cnt) {
       const PlainLoad<KeyT> ld(xk);
       const SmemArray<KeyT> yka(yk + s);
