@@ -428,86 +428,6 @@ __device__ __forceinline__ void merge_thread(int s, const Ld& ld, Cmp cmp, const
   }
 }
 
-// Warp-cooperative merge of one warp's output range [pos, end) of a level
-// (keys-only; equal keys are bit-identical, so tie order is not observable).
-//
-// Per round the warp loads the next 32 keys of run A (lane i: A[ia+i]) and of
-// run B in reverse (lane i: B[ib+31-i]) -- both contiguous, so no bank
-// conflicts.  The elementwise minimum (A wins ties) is exactly the next 32
-// outputs, as a bitonic sequence; five shuffle half-cleaner stages sort it;
-// one ballot counts how many came from A.  Near run ends missing keys count as
-// +infinity through validity flags (a uniform slow path).  One merge-path
-// search per warp (all lanes probe the same addresses: broadcast reads).
-template <class KeyT, class Ld, class Cmp, class PairOf>
-__device__ __forceinline__ void warp_merge_range(int pos, int end, const Ld& ld, uint32_t dst_base,
-                                                 const PairOf& pair_of, Cmp cmp) {
-  constexpr uint32_t S = sizeof(KeyT);
-  const int lane = threadIdx.x & 31;
-  if (pos >= end) return;
-  PairRange P = pair_of(pos);
-  int na = P.ea - P.a0, nb = P.eb - P.b0;
-  uint32_t A0 = ld.addr(P.a0), B0 = ld.addr(P.b0);
-  int ia = merge_path<KeyT>(ld, A0, na, B0, nb, pos - P.out0, cmp);
-  int ib = (pos - P.out0) - ia;
-  while (pos < end) {
-    const int rem = (na - ia) + (nb - ib);
-    int cnt = rem < 32 ? rem : 32;
-    cnt = (end - pos) < cnt ? (end - pos) : cnt;
-    KeyT x;
-    unsigned bal;
-    if (ia + 32 <= na && ib + 32 <= nb) {
-      const KeyT av = ld.at(A0 + (uint32_t)(ia + lane) * S);
-      const KeyT bv = ld.at(B0 + (uint32_t)(ib + 31 - lane) * S);
-      const bool ta = !cmp(bv, av);
-      x = ta ? av : bv;
-      bal = __ballot_sync(0xffffffffu, ta);
-#pragma unroll
-      for (int m = 16; m >= 1; m >>= 1) {
-        const KeyT y = __shfl_xor_sync(0xffffffffu, x, m);
-        const bool y_lt = cmp(y, x);
-        const bool upper = (lane & m) != 0;
-        x = (upper != y_lt) ? y : x;  // lower keeps the min, upper the max
-      }
-    } else {
-      const bool va = ia + lane < na;
-      const bool vb = ib + 31 - lane < nb && ib + 31 - lane >= 0;
-      const KeyT av = ld.at(A0 + (uint32_t)(va ? ia + lane : 0) * S);
-      const KeyT bv = ld.at(B0 + (uint32_t)(vb ? ib + 31 - lane : 0) * S);
-      const bool ta = va && (!vb || !cmp(bv, av));
-      x = ta ? av : bv;
-      bool vx = va || vb;
-      bal = __ballot_sync(0xffffffffu, ta);
-#pragma unroll
-      for (int m = 16; m >= 1; m >>= 1) {
-        const KeyT y = __shfl_xor_sync(0xffffffffu, x, m);
-        const bool vy = __shfl_xor_sync(0xffffffffu, vx, m);
-        const bool y_lt = vy && (!vx || cmp(y, x));
-        const bool x_lt = vx && (!vy || cmp(x, y));
-        const bool upper = (lane & m) != 0;
-        const bool take_y = upper ? x_lt : y_lt;
-        x = take_y ? y : x;
-        vx = take_y ? vy : vx;
-      }
-    }
-    if (lane < cnt) sts<KeyT>(dst_base + (uint32_t)(pos + lane) * S, x);
-    pos += cnt;
-    if (cnt == 32 && cnt < rem) {
-      const int ta_n = __popc(bal);
-      ia += ta_n;
-      ib += 32 - ta_n;
-    } else if (cnt == rem && pos < end) {
-      // pair finished: continue with the pair holding `pos`
-      P = pair_of(pos);
-      na = P.ea - P.a0;
-      nb = P.eb - P.b0;
-      A0 = ld.addr(P.a0);
-      B0 = ld.addr(P.b0);
-      ia = 0;
-      ib = 0;
-    }
-  }
-}
-
 // Largest pair index p (< npairs) whose start pre[p*span] is <= q.
 __device__ __forceinline__ int find_pair(const int* pre, int npairs, int span, int q) {
   int lo = 0, hi = npairs - 1;

@@ -81,6 +81,15 @@ __device__ __forceinline__ KeyT maybe_dec(KeyT x, int on) {
   return on ? Codec::dec(x) : x;
 }
 
+// Comparator on raw user bits that encodes both sides first (when `on`).
+template <class Cmp, class Codec>
+struct EncCmp {
+  int on;
+  template <class KeyT>
+  __device__ __forceinline__ bool operator()(const KeyT& x, const KeyT& y) const {
+    return Cmp()(maybe_enc<Codec>(x, on), maybe_enc<Codec>(y, on));
+  }
+};
 
 // ---------------------------------------------------------------------------
 // The tile kernel.
@@ -398,15 +407,16 @@ __global__ void __launch_bounds__(NT) base_warp_kernel(TileArgs<KeyT, NoVal> a) 
   // shared-memory merge levels: runs of WARP_RUN ... TILE/2
   int cur = 0;
   const int s = tid * ITEMS_M;
-  (void)s;
-  constexpr int WR = TILE / (NT / 32);  // outputs per warp per level
   for (int rl = Geo::WARP_RUN; rl < TILE; rl *= 2) {
     const KeyT* xk = cur ? k1 : k0;
     KeyT* yk = cur ? k0 : k1;
-    const PlainLoad<KeyT> ld(xk);
-    const RegularPairs pairs{rl, TILE};
-    warp_merge_range<KeyT>(warp * WR, warp * WR + WR, ld, static_cast<uint32_t>(__cvta_generic_to_shared(yk)), pairs,
-                           cmp);
+    if (tid < Geo::MERGE_THREADS) {
+      const PlainLoad<KeyT> ld(xk);
+      const SmemArray<KeyT> yka(yk + s);
+      const RegularPairs pairs{rl, TILE};
+      merge_thread<ITEMS_M, KeyT>(s, ld, cmp, pairs,
+                                  [&](int i, KeyT k, uint32_t, bool, const PairRange&) { yka.put(i, k); });
+    }
     __syncthreads();
     cur ^= 1;
   }
@@ -628,28 +638,8 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
   const int64_t run_index = meta[2];
   const int s = tid * ITEMS;
 
-  // Keys-only tiles merge warp-cooperatively: each warp owns a contiguous
-  // range of every level's output.
-  constexpr int kWarps = NT / 32;
-  const int wrange = ((cnt + kWarps - 1) / kWarps + 31) & ~31;
-  const int wbeg = min(cnt, (tid >> 5) * wrange);
-  const int wend = min(cnt, wbeg + wrange);
   // ---- level 1: staged segment pairs -> merge buffer ----
-  if constexpr (!kHasVal) {
-    const int npairs = (nk + 1) / 2;
-    const EncLoad<KeyT, Codec> ld(reinterpret_cast<const KeyT*>(stage_k), a.enc_on_load);
-    auto pair_of = [&](int q) -> PairRange {
-      const int p = find_pair(cpre, npairs, 2, q);
-      const int ka_ = 2 * p;
-      const int kb_ = min(2 * p + 1, nk);
-      const int na = cpre[ka_ + 1] - cpre[ka_];
-      const int nb = (kb_ < nk) ? cpre[kb_ + 1] - cpre[kb_] : 0;
-      const int a0 = sbk[ka_];
-      const int b0 = (kb_ < nk) ? sbk[kb_] : a0 + na;
-      return PairRange{cpre[ka_], a0, a0 + na, b0, b0 + nb, p};
-    };
-    warp_merge_range<KeyT>(wbeg, wend, ld, static_cast<uint32_t>(__cvta_generic_to_shared(k1)), pair_of, cmp);
-  } else if (s < cnt) {
+  if (s < cnt) {
     const int npairs = (nk + 1) / 2;
     const EncLoad<KeyT, Codec> ld(reinterpret_cast<const KeyT*>(stage_k), a.enc_on_load);
     auto pair_of = [&](int q) -> PairRange {
@@ -683,11 +673,7 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
     KeyT* yk = (cur ? k0 : k1);
     const V* xv = (cur ? v1 : v0);
     V* yv = (cur ? v0 : v1);
-    if constexpr (!kHasVal) {
-      const PlainLoad<KeyT> ld(xk);
-      const CompactPairs pairs{cpre, nk, span, (nk + span - 1) >> (31 - __clz(span))};
-      warp_merge_range<KeyT>(wbeg, wend, ld, static_cast<uint32_t>(__cvta_generic_to_shared(yk)), pairs, cmp);
-    } else if (s < cnt) {
+    if (s < cnt) {
       const PlainLoad<KeyT> ld(xk);
       const SmemArray<KeyT> yka(yk + s);
       const SmemArray<V> xva(xv), yva(yv + s);
