@@ -28,6 +28,10 @@ int set_error(int status, const char* msg);
 int cuda_error(cudaError_t e, const char* where);
 void clear_error();
 
+// Instrumentation must not record events while a stream is being captured.
+int timing_suspend();
+void timing_resume(int was_on);
+
 // Scratch cache.  `tag` separates independent buffers of one call.
 void* cache_get(int tag, size_t bytes, cudaStream_t st, int* status);
 

@@ -125,6 +125,20 @@ void after_launch(int kc, cudaStream_t st) {
   g_pending.push_back(TimedLaunch{kc, g_open[kc], b});
 }
 gms::Hooks g_hook_table{before_launch, after_launch};
+}  // namespace
+
+int timing_suspend() {
+  std::lock_guard<std::mutex> g(g_prof_mu);
+  const int was = g_timing;
+  g_timing = 0;
+  return was;
+}
+void timing_resume(int was_on) {
+  std::lock_guard<std::mutex> g(g_prof_mu);
+  g_timing = was_on;
+}
+
+namespace {
 struct InstallHooks {
   InstallHooks() { gms::g_hooks = &g_hook_table; }
 } g_install_hooks;

@@ -28,7 +28,8 @@ INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC"]
-UNITS = ["gms_capi_misc.cu", "gms_capi_k32.cu", "gms_capi_k64.cu", "gms_capi_kv.cu", "gms_capi_noalloc.cu"]
+UNITS = ["gms_capi_misc.cu", "gms_capi_k32.cu", "gms_capi_k64.cu", "gms_capi_kv.cu", "gms_capi_noalloc.cu",
+         "gms_capi_seg.cu"]
 
 GMS_OK = 0
 DTYPES = {"int32": 0, "uint32": 1, "float32": 2, "int64": 3, "uint64": 4, "float64": 5}
@@ -109,6 +110,13 @@ SIGNATURES = {
     "gms_sort_host_i32": (_i32, [_vp, _vp, _i64, _vp]),
     "gms_sort_i32_noalloc": (_i32, [_vp, _vp, _i64, _vp]),
     "gms_sort_host_kv_u64_i32": (_i32, [_vp, _vp, _vp, _vp, _i64, _vp]),
+    "gms_segmented_sort_i32": (_i32, [_vp, _vp, _i64, _vp, _i64, _vp]),
+    "gms_segmented_sort_u32": (_i32, [_vp, _vp, _i64, _vp, _i64, _vp]),
+    "gms_segmented_sort_f32": (_i32, [_vp, _vp, _i64, _vp, _i64, _vp]),
+    "gms_graph_create_sort_i32": (_i32, [_vp, _vp, _i64, _vp, ctypes.POINTER(_vp)]),
+    "gms_graph_create_segmented_i32": (_i32, [_vp, _vp, _i64, _vp, _i64, _vp, ctypes.POINTER(_vp)]),
+    "gms_graph_launch": (_i32, [_vp, _vp]),
+    "gms_graph_destroy": (_i32, [_vp]),
     "gms_tile_sort_i32": (_i32, [_vp, _i64, _i64, _vp]),
     "gms_tile_sort_u64": (_i32, [_vp, _i64, _i64, _vp]),
     "gms_max_tile": (_i64, []),

@@ -162,6 +162,42 @@ int gms_find_partitions_i32(const int32_t* task, int64_t size, int k, int64_t ta
                             int64_t nranks, int64_t* out, void* stream);
 
 /* ---------------------------------------------------------------------------
+ * Batched (segmented) sorts: `n` keys forming `nseg` independent arrays;
+ * array s is [offsets[s], offsets[s+1]) with offsets[0] = 0 and
+ * offsets[nseg] = n (device int64, nseg+1 entries; empty arrays allowed).
+ * Every array is sorted into the same range of `output`; `input` is not
+ * modified.  One sort of 64-bit (array, key) composites sorts them all: every
+ * round is one launch over all arrays.  Bad offsets set bit 3 of the device
+ * status word (gms_device_status).
+ *
+ * No counterpart in the reference: GPU-MMS sorts one array per
+ * multimergesort call (src/multimergesort.hxx:56-141).
+ * ------------------------------------------------------------------------- */
+int gms_segmented_sort_i32(int32_t* input, int32_t* output, int64_t n, const int64_t* offsets, int64_t nseg,
+                           void* stream);
+int gms_segmented_sort_u32(uint32_t* input, uint32_t* output, int64_t n, const int64_t* offsets, int64_t nseg,
+                           void* stream);
+int gms_segmented_sort_f32(float* input, float* output, int64_t n, const int64_t* offsets, int64_t nseg,
+                           void* stream);
+
+/* ---------------------------------------------------------------------------
+ * CUDA graphs: capture the whole launch sequence of one sort (fixed pointers
+ * and sizes) and replay it with a single cudaGraphLaunch.  Creation runs the
+ * sort once outside capture (setting kernel attributes and sizing scratch;
+ * `input` is clobbered as by any sort), then captures it on `stream` (which
+ * must not be the legacy default stream).  Replaying re-sorts whatever
+ * `input` then holds into `output`.
+ * No counterpart in the reference (it launches every kernel from the host
+ * loop, src/multimergesort.hxx:87-135).
+ * ------------------------------------------------------------------------- */
+typedef struct gms_graph gms_graph;
+int gms_graph_create_sort_i32(int32_t* input, int32_t* output, int64_t n, void* stream, gms_graph** graph);
+int gms_graph_create_segmented_i32(int32_t* input, int32_t* output, int64_t n, const int64_t* offsets,
+                                   int64_t nseg, void* stream, gms_graph** graph);
+int gms_graph_launch(gms_graph* graph, void* stream);
+int gms_graph_destroy(gms_graph* graph);
+
+/* ---------------------------------------------------------------------------
  * Scratch management.  Sorts draw device scratch from a per-(device, stream)
  * cache that grows on demand; reserve it ahead of CUDA-graph capture with
  * gms_reserve().  gms_release_workspaces() frees every cached buffer (call it
