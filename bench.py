@@ -134,6 +134,180 @@ def cpu_baseline(orc, n_sample, reps=3):
             f"(__gnu_parallel) on {int(used)} threads, best of {reps}"}
 
 
+def log_uniform_lengths(rng, lo, hi, total_cap=None, count=None):
+    """Segment lengths log-uniform in [lo, hi] until `count` or `total_cap`."""
+    import numpy as np
+
+    out = []
+    tot = 0
+    while True:
+        if count is not None and len(out) >= count:
+            break
+        v = int(np.exp(rng.uniform(np.log(lo), np.log(hi + 1))))
+        v = min(max(v, lo), hi)
+        if total_cap is not None and tot + v > total_cap:
+            break
+        out.append(v)
+        tot += v
+    return np.array(out, dtype=np.int64)
+
+
+def batched_bench(lib, orc, total_keys, nseg=None, seed=7):
+    """Config 4: many int32 arrays, lengths log-uniform in [32, 2^20]; one
+    batched (segmented) sort vs its CUDA-graph replay vs one plain call per
+    array, all device-resident, bit-exact per array."""
+    import numpy as np
+    import torch
+
+    rng = np.random.default_rng(seed)
+    lengths = log_uniform_lengths(rng, 32, 1 << 20, total_cap=total_keys, count=nseg)
+    off = np.zeros(len(lengths) + 1, dtype=np.int64)
+    np.cumsum(lengths, out=off[1:])
+    n = int(off[-1])
+    keys = torch.from_numpy(orc.gen_i32(n, 0, seed)).cuda()
+    toff = torch.from_numpy(off).cuda()
+    out = torch.empty_like(keys)
+    s = torch.cuda.Stream()
+    sp = ctypes.c_void_p(s.cuda_stream)
+
+    def ev_time(fn, reps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(s):
+            fn()  # warm-up
+            s.synchronize()
+            e0.record(s)
+            for _ in range(reps):
+                fn()
+            e1.record(s)
+            s.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    def batched():
+        assert lib.gms_segmented_sort_i32(keys.data_ptr(), out.data_ptr(), n, toff.data_ptr(), len(lengths), sp) == 0
+
+    t_batched = ev_time(batched, 3)
+    batched_out = out.clone()
+    g = ctypes.c_void_p()
+    with torch.cuda.stream(s):
+        assert lib.gms_graph_create_segmented_i32(keys.data_ptr(), out.data_ptr(), n, toff.data_ptr(), len(lengths),
+                                                  sp, ctypes.byref(g)) == 0
+    t_graph = ev_time(lambda: lib.gms_graph_launch(g, sp), 3)
+    lib.gms_graph_destroy(g)
+    # plain: one gms_sort_i32 call per array (input copies made beforehand)
+    work = keys.clone()
+    plain_out = torch.empty_like(keys)
+
+    def plain():
+        for i in range(len(lengths)):
+            a = int(off[i])
+            m = int(lengths[i])
+            assert lib.gms_sort_i32(work.data_ptr() + 4 * a, plain_out.data_ptr() + 4 * a, m, 0, sp) == 0
+
+    with torch.cuda.stream(s):
+        work.copy_(keys)
+    t_plain = ev_time(lambda: (work.copy_(keys), plain()), 1) - ev_time(lambda: work.copy_(keys), 3)
+    same = bool(torch.equal(plain_out, batched_out))
+    return {
+        "workload": f"{len(lengths)} int32 arrays, lengths log-uniform in [32, 2^20], {n} keys in all, uniform keys",
+        "keys": n, "arrays": int(len(lengths)),
+        "batched_gkeys_s": round(n / t_batched / 1e6, 3), "batched_ms": round(t_batched, 3),
+        "graph_gkeys_s": round(n / t_graph / 1e6, 3), "graph_ms": round(t_graph, 3),
+        "plain_calls_gkeys_s": round(n / t_plain / 1e6, 3), "plain_calls_ms": round(t_plain, 3),
+        "speedup_vs_plain": round(t_plain / min(t_batched, t_graph), 2),
+        "bit_exact_vs_plain": same,
+    }
+
+
+def serving_bench(lib, orc, seconds, rate=2000.0, lo=1 << 10, hi=1 << 26, budget=64 << 30, seed=9):
+    """Config 5: Poisson arrivals, sizes log-uniform in [lo, hi], 70% int32 /
+    30% uint64 key + int32 payload, device-resident inputs, admission by a
+    device-memory budget, continuous batching; p50/p99 latency and keys/s vs
+    the same requests sorted by serial plain calls."""
+    import numpy as np
+    import torch
+
+    rng = np.random.default_rng(seed)
+    pool32 = torch.from_numpy(orc.gen_i32(1 << 28, 0, seed)).cuda()
+    pool64 = torch.from_numpy(orc.gen_u64(1 << 27, seed).view(np.int64)).cuda()
+    poolv = torch.arange(1 << 27, dtype=torch.int32, device="cuda")
+    t = 0.0
+    reqs = []
+    while t < seconds:
+        t += rng.exponential(1.0 / rate)
+        n = int(np.exp(rng.uniform(np.log(lo), np.log(hi + 1))))
+        n = min(max(n, lo), hi)
+        kind = 0 if rng.uniform() < 0.7 else 1
+        cap = (1 << 28) if kind == 0 else (1 << 27)
+        n = min(n, cap)
+        o = int(rng.integers(0, cap - n + 1))
+        reqs.append((t, kind, n, o))
+    torch.cuda.synchronize()
+    srv = ctypes.c_void_p()
+    assert lib.gms_server_create(budget, 8, 1 << 16, hi, ctypes.byref(srv)) == 0, lib.gms_last_error()
+    outs = {}
+    ids = []
+    t0 = time.perf_counter()
+    for (ta, kind, n, o) in reqs:
+        now = time.perf_counter() - t0
+        if ta > now:
+            time.sleep(ta - now)
+        if kind == 0:
+            ko = torch.empty(n, dtype=torch.int32, device="cuda")
+            kin, vin, vo = pool32.data_ptr() + 4 * o, None, None
+        else:
+            ko = torch.empty(n, dtype=torch.int64, device="cuda")
+            vo_t = torch.empty(n, dtype=torch.int32, device="cuda")
+            kin, vin, vo = pool64.data_ptr() + 8 * o, poolv.data_ptr() + 4 * o, vo_t.data_ptr()
+            outs[len(ids), "v"] = vo_t
+        rid = ctypes.c_uint64()
+        assert lib.gms_server_submit(srv, kind, kin, vin, ko.data_ptr(), vo, n, ctypes.byref(rid)) == 0
+        outs[len(ids)] = ko
+        ids.append(rid.value)
+    assert lib.gms_server_drain(srv) == 0, lib.gms_last_error()
+    wall = time.perf_counter() - t0
+    done = ctypes.c_int64()
+    p50, p99, kps = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    lib.gms_server_stats(srv, ctypes.byref(done), ctypes.byref(p50), ctypes.byref(p99), ctypes.byref(kps))
+    for rid in ids:
+        lib.gms_server_wait(srv, rid, None)
+    lib.gms_server_destroy(srv)
+    outs.clear()
+    keys_total = sum(r[2] for r in reqs)
+    # the same requests, serially, one plain call each (device-resident)
+    s = torch.cuda.Stream()
+    sp = ctypes.c_void_p(s.cuda_stream)
+    tmp32 = torch.empty(hi, dtype=torch.int32, device="cuda")
+    out32 = torch.empty_like(tmp32)
+    tmp64 = torch.empty(min(hi, 1 << 27), dtype=torch.int64, device="cuda")
+    out64 = torch.empty_like(tmp64)
+    tmpv = torch.empty(min(hi, 1 << 27), dtype=torch.int32, device="cuda")
+    outv = torch.empty_like(tmpv)
+    torch.cuda.synchronize()
+    ts = time.perf_counter()
+    with torch.cuda.stream(s):
+        for (_, kind, n, o) in reqs:
+            if kind == 0:
+                tmp32[:n].copy_(pool32[o:o + n])
+                assert lib.gms_sort_i32(tmp32.data_ptr(), out32.data_ptr(), n, 0, sp) == 0
+            else:
+                tmp64[:n].copy_(pool64[o:o + n])
+                tmpv[:n].copy_(poolv[o:o + n])
+                assert lib.gms_sort_kv_u64_i32(tmp64.data_ptr(), tmpv.data_ptr(), out64.data_ptr(), outv.data_ptr(),
+                                               n, 0, sp) == 0
+        s.synchronize()
+    serial = time.perf_counter() - ts
+    return {
+        "workload": f"Poisson {rate:.0f} req/s for {seconds} s, sizes log-uniform [{lo}, {hi}], 70% int32 / 30% "
+                    f"uint64+int32, {budget >> 30} GB budget, 8 streams, batching <= 65536 keys",
+        "requests": len(reqs), "completed": int(done.value), "keys": keys_total,
+        "p50_ms": round(p50.value, 3), "p99_ms": round(p99.value, 3),
+        "served_gkeys_s": round(kps.value / 1e9, 3), "wall_s": round(wall, 3),
+        "serial_plain_gkeys_s": round(keys_total / serial / 1e9, 3), "serial_plain_s": round(serial, 3),
+        "speedup_vs_serial": round(serial / max(wall, 1e-9), 2),
+    }
+
+
 def run_reference(args):
     """CPU arm: the oracle's std::sort with every host thread."""
     import numpy as np
@@ -336,6 +510,11 @@ def run_ours(args):
     }
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(orc, min(n, 1 << 26))
+    if not args.no_extra:
+        del inputs
+        torch.cuda.empty_cache()
+        line["batched"] = batched_bench(lib, orc, total_keys=1 << 27)
+        line["serving"] = serving_bench(lib, orc, seconds=2.0)
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -350,11 +529,30 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-extra", action="store_true", help="skip the batched and serving sections")
+    ap.add_argument("--mode", default="sort", choices=["sort", "batched", "serve"],
+                    help="sort: the headline line; batched / serve: the full-size config 4 / config 5 runs")
+    ap.add_argument("--seconds", type=float, default=60.0, help="serve mode: arrival window")
+    ap.add_argument("--segments", type=int, default=50000, help="batched mode: number of arrays")
     args = ap.parse_args()
     if args.steps < 1 or args.warmup < 0:
         ap.error("steps >= 1, warmup >= 0")
     if args.impl == "reference":
         return run_reference(args)
+    if args.mode != "sort":
+        import torch
+        from conftest import Oracle, load_gms_module
+
+        gms = load_gms_module()
+        gms.build()
+        lib = gms.load()
+        orc = Oracle()
+        if args.mode == "batched":
+            res = batched_bench(lib, orc, total_keys=None, nseg=args.segments)
+        else:
+            res = serving_bench(lib, orc, seconds=args.seconds)
+        print(json.dumps({"mode": args.mode, **res}), flush=True)
+        return 0
     return run_ours(args)
 
 

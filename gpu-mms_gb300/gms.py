@@ -29,7 +29,7 @@ INCLUDE = os.path.join(ROOT, "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC"]
 UNITS = ["gms_capi_misc.cu", "gms_capi_k32.cu", "gms_capi_k64.cu", "gms_capi_kv.cu", "gms_capi_noalloc.cu",
-         "gms_capi_seg.cu"]
+         "gms_capi_seg.cu", "gms_server.cu"]
 
 GMS_OK = 0
 DTYPES = {"int32": 0, "uint32": 1, "float32": 2, "int64": 3, "uint64": 4, "float64": 5}
@@ -116,6 +116,13 @@ SIGNATURES = {
     "gms_graph_create_sort_i32": (_i32, [_vp, _vp, _i64, _vp, ctypes.POINTER(_vp)]),
     "gms_graph_create_segmented_i32": (_i32, [_vp, _vp, _i64, _vp, _i64, _vp, ctypes.POINTER(_vp)]),
     "gms_graph_launch": (_i32, [_vp, _vp]),
+    "gms_server_create": (_i32, [_sz, _i32, _i64, _i64, ctypes.POINTER(_vp)]),
+    "gms_server_submit": (_i32, [_vp, _i32, _vp, _vp, _vp, _vp, _i64, ctypes.POINTER(ctypes.c_uint64)]),
+    "gms_server_wait": (_i32, [_vp, ctypes.c_uint64, ctypes.POINTER(ctypes.c_double)]),
+    "gms_server_drain": (_i32, [_vp]),
+    "gms_server_stats": (_i32, [_vp, ctypes.POINTER(_i64), ctypes.POINTER(ctypes.c_double),
+                                ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
+    "gms_server_destroy": (_i32, [_vp]),
     "gms_graph_destroy": (_i32, [_vp]),
     "gms_tile_sort_i32": (_i32, [_vp, _i64, _i64, _vp]),
     "gms_tile_sort_u64": (_i32, [_vp, _i64, _i64, _vp]),

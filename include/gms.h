@@ -198,12 +198,44 @@ int gms_graph_launch(gms_graph* graph, void* stream);
 int gms_graph_destroy(gms_graph* graph);
 
 /* ---------------------------------------------------------------------------
+ * Sort server: continuous batching of device-resident requests.
+ * No counterpart in the reference (a synchronous one-call-per-array library,
+ * src/multimergesort.hxx:56-141).
+ *
+ * gms_server_create starts a dispatcher and a completion thread on the current
+ * device with `nstreams` streams.  Requests (gms_server_submit) are device
+ * buffers: kind 0 = int32 keys, kind 1 = uint64 keys + int32 payload (stable);
+ * inputs are never modified; results go to the caller's output buffers.
+ * int32 requests of at most `batch_max_keys` keys that wait together are
+ * sorted as ONE batched sort; larger and key/value requests run one per work
+ * item.  A work item starts only when its staging memory (stream-ordered
+ * cudaMallocAsync) fits what is left of `memory_budget`; items run on the
+ * stream pool concurrently while new requests keep arriving.  Each stream's
+ * sort scratch is reserved at creation for `max_request_keys` keys (outside
+ * the budget), so nothing allocates with cudaMalloc while serving.
+ * gms_server_wait blocks until one request is done and gives its latency
+ * (submit to completion); gms_server_stats reports p50/p99 latency and keys/s.
+ * ------------------------------------------------------------------------- */
+typedef struct gms_server gms_server;
+int gms_server_create(size_t memory_budget, int nstreams, int64_t batch_max_keys, int64_t max_request_keys,
+                      gms_server** server);
+int gms_server_submit(gms_server* server, int kind, const void* keys_in, const int32_t* vals_in, void* keys_out,
+                      int32_t* vals_out, int64_t n, uint64_t* request_id);
+int gms_server_wait(gms_server* server, uint64_t request_id, double* latency_ms);
+int gms_server_drain(gms_server* server);
+int gms_server_stats(gms_server* server, int64_t* completed, double* p50_ms, double* p99_ms, double* keys_per_s);
+int gms_server_destroy(gms_server* server);
+
+/* ---------------------------------------------------------------------------
  * Scratch management.  Sorts draw device scratch from a per-(device, stream)
  * cache that grows on demand; reserve it ahead of CUDA-graph capture with
  * gms_reserve().  gms_release_workspaces() frees every cached buffer (call it
  * only when no sort is in flight).
  * ------------------------------------------------------------------------- */
-/* dtype codes: 0=i32 1=u32 2=f32 3=i64 4=u64 5=f64; kv: 1 = with int32 payload */
+/* dtype codes: 0=i32 1=u32 2=f32 3=i64 4=u64 5=f64; kv: 1 = with int32 payload.
+ * gms_reserve also accepts GMS_RESERVE_SEGMENTED_I32 (batched 32-bit sorts of
+ * up to n keys in all). */
+#define GMS_RESERVE_SEGMENTED_I32 6
 size_t gms_workspace_bytes(int dtype, int kv, int64_t n);
 int gms_reserve(int dtype, int kv, int64_t n, void* stream);
 void gms_release_workspaces(void);
