@@ -228,13 +228,17 @@ def serving_bench(lib, orc, seconds, rate=2000.0, lo=1 << 10, hi=1 << 26, budget
     import torch
 
     rng = np.random.default_rng(seed)
+    count = None
+    if rate <= 0:
+        # capacity run: as many requests as 2000 req/s would bring, all at t=0
+        count = int(2000 * seconds)
     pool32 = torch.from_numpy(orc.gen_i32(1 << 28, 0, seed)).cuda()
     pool64 = torch.from_numpy(orc.gen_u64(1 << 27, seed).view(np.int64)).cuda()
     poolv = torch.arange(1 << 27, dtype=torch.int32, device="cuda")
     t = 0.0
     reqs = []
-    while t < seconds:
-        t += rng.exponential(1.0 / rate)
+    while (t < seconds) if count is None else (len(reqs) < count):
+        t = t + rng.exponential(1.0 / rate) if count is None else 0.0
         n = int(np.exp(rng.uniform(np.log(lo), np.log(hi + 1))))
         n = min(max(n, lo), hi)
         kind = 0 if rng.uniform() < 0.7 else 1
@@ -305,8 +309,10 @@ def serving_bench(lib, orc, seconds, rate=2000.0, lo=1 << 10, hi=1 << 26, budget
         s.synchronize()
     serial = time.perf_counter() - ts
     return {
-        "workload": f"Poisson {rate:.0f} req/s for {seconds} s, sizes log-uniform [{lo}, {hi}], 70% int32 / 30% "
-                    f"uint64+int32, {budget >> 30} GB budget, 8 streams, batching <= 65536 keys",
+        "workload": (f"Poisson {rate:.0f} req/s for {seconds} s" if count is None else
+                     f"{count} requests all arriving at once (capacity)") +
+                    f", sizes log-uniform [{lo}, {hi}], 70% int32 / 30% uint64+int32, {budget >> 30} GB budget, "
+                    "8 streams, batching <= 65536 keys",
         "requests": len(reqs), "completed": int(done.value), "keys": keys_total,
         "p50_ms": round(p50.value, 3), "p99_ms": round(p99.value, 3),
         "served_gkeys_s": round(kps.value / 1e9, 3), "wall_s": round(wall, 3),
@@ -522,6 +528,8 @@ def run_ours(args):
         torch.cuda.empty_cache()
         line["batched"] = batched_bench(lib, orc, total_keys=1 << 27)
         line["serving"] = serving_bench(lib, orc, seconds=2.0)
+        line["serving_capacity"] = serving_bench(lib, orc, seconds=2.0, rate=0)
+        line["serving_small"] = serving_bench(lib, orc, seconds=1.0, rate=20000.0, hi=1 << 16)
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -537,8 +545,11 @@ def main():
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-extra", action="store_true", help="skip the batched and serving sections")
-    ap.add_argument("--mode", default="sort", choices=["sort", "batched", "serve"],
-                    help="sort: the headline line; batched / serve: the full-size config 4 / config 5 runs")
+    ap.add_argument("--mode", default="sort", choices=["sort", "batched", "serve", "profile"],
+                    help="sort: the headline line; batched / serve: the full-size config 4 / config 5 runs; "
+                         "profile: warm-up sorts plus one sort of --n keys and nothing else (for ncu)")
+    ap.add_argument("--rate", type=float, default=2000.0, help="serve mode: arrivals per second (0: all at once)")
+    ap.add_argument("--max-size", type=int, default=1 << 26, help="serve mode: largest request (keys)")
     ap.add_argument("--seconds", type=float, default=60.0, help="serve mode: arrival window")
     ap.add_argument("--segments", type=int, default=50000, help="batched mode: number of arrays")
     args = ap.parse_args()
@@ -554,10 +565,21 @@ def main():
         gms.build()
         lib = gms.load()
         orc = Oracle()
+        if args.mode == "profile":
+            n = args.n
+            src = torch.from_numpy(orc.gen_i32(n, 0, SEED)).cuda()
+            tin, tout = torch.empty_like(src), torch.empty_like(src)
+            sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+            for _ in range(args.warmup + 1):
+                tin.copy_(src)
+                assert lib.gms_sort_i32(tin.data_ptr(), tout.data_ptr(), n, 0, sp) == 0
+            torch.cuda.synchronize()
+            print(json.dumps({"mode": "profile", "n": n, "sorts": args.warmup + 1}), flush=True)
+            return 0
         if args.mode == "batched":
             res = batched_bench(lib, orc, total_keys=None, nseg=args.segments)
         else:
-            res = serving_bench(lib, orc, seconds=args.seconds)
+            res = serving_bench(lib, orc, seconds=args.seconds, rate=args.rate, hi=args.max_size)
         print(json.dumps({"mode": args.mode, **res}), flush=True)
         return 0
     return run_ours(args)

@@ -24,6 +24,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgms.so")
+CLI = os.path.join(HERE, "testmm")
 INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -52,7 +53,7 @@ def _nvcc():
 
 def _sources():
     out = []
-    for d in (CSRC, INCLUDE):
+    for d in (CSRC, INCLUDE, os.path.join(HERE, "cli")):
         for f in os.listdir(d):
             if f.endswith((".cu", ".cuh", ".h", ".hxx")):
                 out.append(os.path.join(d, f))
@@ -77,8 +78,19 @@ def build(force=False, jobs=None, verbose=False):
             print(r.stdout, r.stderr)
         return obj
 
-    with ThreadPoolExecutor(max_workers=jobs or len(UNITS)) as ex:
+    def compile_cli():
+        # testmm: the reference-compatible command-line driver (header-only path)
+        cmd = [nvcc] + ARCH + ["-O2", "-std=c++17", "--expt-relaxed-constexpr", "-I", INCLUDE,
+                               os.path.join(HERE, "cli", "testmm.cu"), "-o", CLI + ".tmp"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed for testmm:\n{r.stdout}\n{r.stderr}")
+        os.replace(CLI + ".tmp", CLI)
+
+    with ThreadPoolExecutor(max_workers=jobs or len(UNITS) + 1) as ex:
+        cli = ex.submit(compile_cli)
         objs = list(ex.map(compile_one, UNITS))
+        cli.result()
     tmp = LIB + ".tmp"
     cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
