@@ -231,7 +231,7 @@ def serving_bench(lib, orc, seconds, rate=2000.0, lo=1 << 10, hi=1 << 26, budget
     count = None
     if rate <= 0:
         # capacity run: as many requests as 2000 req/s would bring, all at t=0
-        count = int(2000 * seconds)
+        count = int((20000 if hi <= (1 << 16) else 2000) * seconds)
     pool32 = torch.from_numpy(orc.gen_i32(1 << 28, 0, seed)).cuda()
     pool64 = torch.from_numpy(orc.gen_u64(1 << 27, seed).view(np.int64)).cuda()
     poolv = torch.arange(1 << 27, dtype=torch.int32, device="cuda")
@@ -530,6 +530,7 @@ def run_ours(args):
         line["serving"] = serving_bench(lib, orc, seconds=2.0)
         line["serving_capacity"] = serving_bench(lib, orc, seconds=2.0, rate=0)
         line["serving_small"] = serving_bench(lib, orc, seconds=1.0, rate=20000.0, hi=1 << 16)
+        line["serving_small_capacity"] = serving_bench(lib, orc, seconds=1.0, rate=0, hi=1 << 16)
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
