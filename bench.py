@@ -392,6 +392,8 @@ def run_ours(args):
     ncopies = max(args.steps, args.warmup)
     inputs = [torch.empty_like(src) for _ in range(ncopies)]
     out = torch.empty_like(src)
+    autotuned = gms.autotune("int32", n, stream=stream) if args.autotune else None
+    tune = gms.tune_for("int32", n)
     assert lib.gms_reserve(0, 0, n, sp) == 0
 
     def refill(k):
@@ -503,8 +505,10 @@ def run_ours(args):
         "data": "synthetic: uniform int32 in [0, 2^31-1), mt19937_64 seed 1 (+rank)",
         "config": {
             "workload": f"multimergesort int32 N={n} uniform, one full sort per step",
-            "n": n, "rounds": rounds, "passes": passes, "base_tile": int(lib.gms_base_tile(0, 0)), "k": 32,
-            "sample_block": 32, "parallelism": "replicas" if ws > 1 else "single",
+            "n": n, "rounds": rounds, "passes": passes, "base_tile": int(lib.gms_base_tile(0, 0)), "k": tune["k"],
+            "sample_block": tune["sample_b"], "bulk_copy": tune["bulk_copy"],
+            "tuning": "autotuned before warm-up" if autotuned else "defaults",
+            "parallelism": "replicas" if ws > 1 else "single",
             "l2": "each step sorts its own 1 GiB input copy (> 129 MB L2)",
             "correct": ok and e2e_ok,
         },
@@ -545,6 +549,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--autotune", action="store_true", help="run gms_autotune for the workload before warm-up")
     ap.add_argument("--no-extra", action="store_true", help="skip the batched and serving sections")
     ap.add_argument("--mode", default="sort", choices=["sort", "batched", "serve", "profile"],
                     help="sort: the headline line; batched / serve: the full-size config 4 / config 5 runs; "

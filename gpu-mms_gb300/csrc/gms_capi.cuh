@@ -35,20 +35,23 @@ void timing_resume(int was_on);
 // Scratch cache.  `tag` separates independent buffers of one call.
 void* cache_get(int tag, size_t bytes, cudaStream_t st, int* status);
 
-// Process-wide tuning (gms_set_tune); defaults are gms::Tune{}.
+// Tuning used by a call: the tuning set with gms_set_tune if the caller set
+// one; else the autotuned entry for (dtype, payload, size class) if there is
+// one; else the defaults gms::Tune{}.
 gms::Tune current_tune();
+gms::Tune tune_for(int dtype, int kv, int64_t n);
 inline gms::Tune default_tune() { return current_tune(); }
 
 // Runs a full sort of one dtype with the scratch cache.
 template <class Eng, class K, class V>
-int run_sort(K* in, V* vin, K* out, V* vout, int64_t n, cudaStream_t st) {
+int run_sort(K* in, V* vin, K* out, V* vout, int64_t n, cudaStream_t st, int dtype) {
   clear_error();
   if (n < 0) return set_error(GMS_ERR_INVALID, "n < 0");
   if (n == 0) return GMS_OK;
   if (!in || !out) return set_error(GMS_ERR_INVALID, "null key pointer");
   if (gms::HasVal<V>::value && (!vin || !vout)) return set_error(GMS_ERR_INVALID, "null value pointer");
   if (n > ((int64_t)1 << 32) * 32) return set_error(GMS_ERR_TOO_LARGE, "n beyond 2^37");
-  const gms::Tune t = default_tune();
+  const gms::Tune t = tune_for(dtype, gms::HasVal<V>::value ? 1 : 0, n);
   const gms::WsLayout l = Eng::plan(n, t);
   if (!l.ok) return set_error(GMS_ERR_INVALID, "tuning too fine for this n (sample recursion too deep)");
   const size_t bytes = gms::ws_bytes_for<K>(l, t.k);
@@ -62,8 +65,8 @@ int run_sort(K* in, V* vin, K* out, V* vout, int64_t n, cudaStream_t st) {
 }
 
 template <class Eng, class K>
-size_t sort_ws_bytes(int64_t n) {
-  const gms::Tune t = default_tune();
+size_t sort_ws_bytes(int64_t n, int dtype, int kv) {
+  const gms::Tune t = tune_for(dtype, kv, n);
   return gms::ws_bytes_for<K>(Eng::plan(n, t), t.k);
 }
 

@@ -11,8 +11,8 @@ using EngU32 = KeysEngine<uint32_t, gms::IdentityCodec<uint32_t>>;
 using EngF32 = KeysEngine<uint32_t, gms::FloatOrder32>;
 
 template <class Eng>
-int sort32(void* in, void* out, int64_t n, void* st) {
-  return run_sort<Eng, uint32_t, NoVal>((uint32_t*)in, nullptr, (uint32_t*)out, nullptr, n, (cudaStream_t)st);
+int sort32(void* in, void* out, int64_t n, void* st, int dtype) {
+  return run_sort<Eng, uint32_t, NoVal>((uint32_t*)in, nullptr, (uint32_t*)out, nullptr, n, (cudaStream_t)st, dtype);
 }
 
 }  // namespace
@@ -21,15 +21,15 @@ extern "C" {
 
 int gms_sort_i32(int32_t* in, int32_t* out, int64_t n, int tb, void* st) {
   (void)tb;
-  return sort32<EngI32>(in, out, n, st);
+  return sort32<EngI32>(in, out, n, st, 0);
 }
 int gms_sort_u32(uint32_t* in, uint32_t* out, int64_t n, int tb, void* st) {
   (void)tb;
-  return sort32<EngU32>(in, out, n, st);
+  return sort32<EngU32>(in, out, n, st, 1);
 }
 int gms_sort_f32(float* in, float* out, int64_t n, int tb, void* st) {
   (void)tb;
-  return sort32<EngF32>(in, out, n, st);
+  return sort32<EngF32>(in, out, n, st, 2);
 }
 
 int gms_tile_sort_i32(int32_t* data, int64_t n, int64_t tile, void* st) {
@@ -111,7 +111,7 @@ int gms_sort_host_i32(const int32_t* host_in, int32_t* host_out, int64_t n, void
   if (status != GMS_OK) return status;
   cudaError_t e = cudaMemcpyAsync(din, host_in, bytes, cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) return cuda_error(e, "cudaMemcpyAsync H2D");
-  status = sort32<EngI32>(din, dout, n, st);
+  status = sort32<EngI32>(din, dout, n, st, 0);
   if (status != GMS_OK) return status;
   e = cudaMemcpyAsync(host_out, dout, bytes, cudaMemcpyDeviceToHost, st);
   if (e != cudaSuccess) return cuda_error(e, "cudaMemcpyAsync D2H");

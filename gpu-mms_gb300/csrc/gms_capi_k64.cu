@@ -11,8 +11,8 @@ using EngU64 = KeysEngine<uint64_t, gms::IdentityCodec<uint64_t>>;
 using EngF64 = KeysEngine<uint64_t, gms::FloatOrder64>;
 
 template <class Eng>
-int sort64(void* in, void* out, int64_t n, void* st) {
-  return run_sort<Eng, uint64_t, NoVal>((uint64_t*)in, nullptr, (uint64_t*)out, nullptr, n, (cudaStream_t)st);
+int sort64(void* in, void* out, int64_t n, void* st, int dtype) {
+  return run_sort<Eng, uint64_t, NoVal>((uint64_t*)in, nullptr, (uint64_t*)out, nullptr, n, (cudaStream_t)st, dtype);
 }
 
 }  // namespace
@@ -21,15 +21,15 @@ extern "C" {
 
 int gms_sort_i64(int64_t* in, int64_t* out, int64_t n, int tb, void* st) {
   (void)tb;
-  return sort64<EngI64>(in, out, n, st);
+  return sort64<EngI64>(in, out, n, st, 3);
 }
 int gms_sort_u64(uint64_t* in, uint64_t* out, int64_t n, int tb, void* st) {
   (void)tb;
-  return sort64<EngU64>(in, out, n, st);
+  return sort64<EngU64>(in, out, n, st, 4);
 }
 int gms_sort_f64(double* in, double* out, int64_t n, int tb, void* st) {
   (void)tb;
-  return sort64<EngF64>(in, out, n, st);
+  return sort64<EngF64>(in, out, n, st, 5);
 }
 
 int gms_tile_sort_u64(uint64_t* data, int64_t n, int64_t tile, void* st) {

@@ -6,8 +6,8 @@ using namespace gms_capi;
 namespace {
 
 template <class Eng, class K>
-int kv(void* ki, int32_t* vi, void* ko, int32_t* vo, int64_t n, void* st) {
-  return run_sort<Eng, K, int32_t>((K*)ki, vi, (K*)ko, vo, n, (cudaStream_t)st);
+int kv(void* ki, int32_t* vi, void* ko, int32_t* vo, int64_t n, void* st, int dtype) {
+  return run_sort<Eng, K, int32_t>((K*)ki, vi, (K*)ko, vo, n, (cudaStream_t)st, dtype);
 }
 
 }  // namespace
@@ -16,27 +16,27 @@ extern "C" {
 
 int gms_sort_kv_i32_i32(int32_t* ki, int32_t* vi, int32_t* ko, int32_t* vo, int64_t n, int tb, void* st) {
   (void)tb;
-  return kv<KvEngine<uint32_t, gms::SignFlip32>, uint32_t>(ki, vi, ko, vo, n, st);
+  return kv<KvEngine<uint32_t, gms::SignFlip32>, uint32_t>(ki, vi, ko, vo, n, st, 0);
 }
 int gms_sort_kv_u32_i32(uint32_t* ki, int32_t* vi, uint32_t* ko, int32_t* vo, int64_t n, int tb, void* st) {
   (void)tb;
-  return kv<KvEngine<uint32_t, gms::IdentityCodec<uint32_t>>, uint32_t>(ki, vi, ko, vo, n, st);
+  return kv<KvEngine<uint32_t, gms::IdentityCodec<uint32_t>>, uint32_t>(ki, vi, ko, vo, n, st, 1);
 }
 int gms_sort_kv_f32_i32(float* ki, int32_t* vi, float* ko, int32_t* vo, int64_t n, int tb, void* st) {
   (void)tb;
-  return kv<KvEngine<uint32_t, gms::FloatOrder32>, uint32_t>(ki, vi, ko, vo, n, st);
+  return kv<KvEngine<uint32_t, gms::FloatOrder32>, uint32_t>(ki, vi, ko, vo, n, st, 2);
 }
 int gms_sort_kv_i64_i32(int64_t* ki, int32_t* vi, int64_t* ko, int32_t* vo, int64_t n, int tb, void* st) {
   (void)tb;
-  return kv<KvEngine<uint64_t, gms::SignFlip64>, uint64_t>(ki, vi, ko, vo, n, st);
+  return kv<KvEngine<uint64_t, gms::SignFlip64>, uint64_t>(ki, vi, ko, vo, n, st, 3);
 }
 int gms_sort_kv_u64_i32(uint64_t* ki, int32_t* vi, uint64_t* ko, int32_t* vo, int64_t n, int tb, void* st) {
   (void)tb;
-  return kv<KvEngine<uint64_t, gms::IdentityCodec<uint64_t>>, uint64_t>(ki, vi, ko, vo, n, st);
+  return kv<KvEngine<uint64_t, gms::IdentityCodec<uint64_t>>, uint64_t>(ki, vi, ko, vo, n, st, 4);
 }
 int gms_sort_kv_f64_i32(double* ki, int32_t* vi, double* ko, int32_t* vo, int64_t n, int tb, void* st) {
   (void)tb;
-  return kv<KvEngine<uint64_t, gms::FloatOrder64>, uint64_t>(ki, vi, ko, vo, n, st);
+  return kv<KvEngine<uint64_t, gms::FloatOrder64>, uint64_t>(ki, vi, ko, vo, n, st, 5);
 }
 
 int gms_sort_host_kv_u64_i32(const uint64_t* keys_in, const int32_t* vals_in, uint64_t* keys_out, int32_t* vals_out,
@@ -60,7 +60,7 @@ int gms_sort_host_kv_u64_i32(const uint64_t* keys_in, const int32_t* vals_in, ui
   if (e == cudaSuccess) e = cudaMemcpyAsync(dvi, vals_in, vb, cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) return cuda_error(e, "cudaMemcpyAsync H2D");
   status = kv<KvEngine<uint64_t, gms::IdentityCodec<uint64_t>>, uint64_t>(dki, (int32_t*)dvi, dko, (int32_t*)dvo, n,
-                                                                         stv);
+                                                                         stv, 4);
   if (status != GMS_OK) return status;
   e = cudaMemcpyAsync(keys_out, dko, kb, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(vals_out, dvo, vb, cudaMemcpyDeviceToHost, st);

@@ -74,16 +74,6 @@ void* cache_get(int tag, size_t bytes, cudaStream_t st, int* status) {
   return p;
 }
 
-// ---- tuning ----
-namespace {
-std::mutex g_tune_mu;
-gms::Tune g_tune;
-}  // namespace
-gms::Tune current_tune() {
-  std::lock_guard<std::mutex> g(g_tune_mu);
-  return g_tune;
-}
-
 // ---- launch counting and live kernel timing ----
 namespace {
 struct TimedLaunch {
@@ -178,26 +168,6 @@ void gms_release_workspaces(void) {
   g_slots.clear();
 }
 
-int gms_set_tune(int k, int sample_b, int bulk_copy) {
-  clear_error();
-  if (k < 2 || k > 32) return set_error(GMS_ERR_INVALID, "k must be in [2, 32]");
-  if (sample_b < 8 || (int64_t)kNT * kItems / sample_b - k < 1)
-    return set_error(GMS_ERR_INVALID, "sample_b must be >= 8 and leave room for a tile (CAP/sample_b > k)");
-  std::lock_guard<std::mutex> g(g_tune_mu);
-  g_tune.k = k;
-  g_tune.sample_b = sample_b;
-  g_tune.bulk_copy = bulk_copy ? 1 : 0;
-  return GMS_OK;
-}
-
-int gms_get_tune(int* k, int* sample_b, int* bulk_copy) {
-  std::lock_guard<std::mutex> g(g_tune_mu);
-  if (k) *k = g_tune.k;
-  if (sample_b) *sample_b = g_tune.sample_b;
-  if (bulk_copy) *bulk_copy = g_tune.bulk_copy;
-  return GMS_OK;
-}
-
 long long gms_launch_count(void) {
   std::lock_guard<std::mutex> g(g_prof_mu);
   long long t = 0;
@@ -251,7 +221,8 @@ int64_t gms_base_tile(int dtype, int kv) {
 
 int gms_rounds(int dtype, int kv, int64_t n) {
   int p = 0;
-  for (int64_t L = gms_base_tile(dtype, kv); L < n; L *= default_tune().k) ++p;
+  const int k = tune_for(dtype, kv, n).k;
+  for (int64_t L = gms_base_tile(dtype, kv); L < n; L *= k) ++p;
   return p;
 }
 
@@ -259,11 +230,11 @@ size_t gms_workspace_bytes(int dtype, int kv, int64_t n) {
   if (n <= 0) return 0;
   const bool wide = (dtype >= 3);
   if (wide) {
-    return kv ? sort_ws_bytes<KvEngine<uint64_t, gms::IdentityCodec<uint64_t>>, uint64_t>(n)
-              : sort_ws_bytes<KeysEngine<uint64_t, gms::IdentityCodec<uint64_t>>, uint64_t>(n);
+    return kv ? sort_ws_bytes<KvEngine<uint64_t, gms::IdentityCodec<uint64_t>>, uint64_t>(n, dtype, kv)
+              : sort_ws_bytes<KeysEngine<uint64_t, gms::IdentityCodec<uint64_t>>, uint64_t>(n, dtype, kv);
   }
-  return kv ? sort_ws_bytes<KvEngine<uint32_t, gms::IdentityCodec<uint32_t>>, uint32_t>(n)
-            : sort_ws_bytes<KeysEngine<uint32_t, gms::IdentityCodec<uint32_t>>, uint32_t>(n);
+  return kv ? sort_ws_bytes<KvEngine<uint32_t, gms::IdentityCodec<uint32_t>>, uint32_t>(n, dtype, kv)
+            : sort_ws_bytes<KeysEngine<uint32_t, gms::IdentityCodec<uint32_t>>, uint32_t>(n, dtype, kv);
 }
 
 int gms_device_status(void* stream, int* status_out) {

@@ -27,7 +27,7 @@ int segmented32(void* in, void* out, int64_t n, const int64_t* off, int64_t nseg
   if (!in || !out || !off) return set_error(GMS_ERR_INVALID, "null pointer");
   if (nseg > 0xffffffffll) return set_error(GMS_ERR_TOO_LARGE, "more than 2^32 segments");
   if (n > ((int64_t)1 << 37)) return set_error(GMS_ERR_TOO_LARGE, "n beyond 2^37");
-  const gms::Tune t = default_tune();
+  const gms::Tune t = tune_for(4, 0, n);  // the composites sort as uint64 keys
   const gms::WsLayout l = CompEngine::plan(n, t);
   if (!l.ok) return set_error(GMS_ERR_INVALID, "tuning too fine for this n (sample recursion too deep)");
   int status = GMS_OK;

@@ -65,7 +65,7 @@ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 struct Tune {
   int k = 32;         // fan-in per round (<= 32)
   int sample_b = 32;  // block size of the forecast sample
-  int bulk_copy = 1;  // 1: persistent merge with bulk-copy staging; 0: one CTA per tile, plain loads
+  int bulk_copy = 1;  // 1: merge with bulk-copy staging of the tile segments; 0: merge with plain loads
 };
 
 // Scratch layout, computed by a dry run of the same recursion as the real run.

@@ -30,7 +30,7 @@ INCLUDE = os.path.join(ROOT, "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC"]
 UNITS = ["gms_capi_misc.cu", "gms_capi_k32.cu", "gms_capi_k64.cu", "gms_capi_kv.cu", "gms_capi_noalloc.cu",
-         "gms_capi_seg.cu", "gms_server.cu"]
+         "gms_capi_seg.cu", "gms_capi_tune.cu", "gms_server.cu"]
 
 GMS_OK = 0
 DTYPES = {"int32": 0, "uint32": 1, "float32": 2, "int64": 3, "uint64": 4, "float64": 5}
@@ -149,6 +149,14 @@ SIGNATURES = {
     "gms_launch_count": (ctypes.c_longlong, []),
     "gms_set_tune": (_i32, [_i32, _i32, _i32]),
     "gms_get_tune": (_i32, [ctypes.POINTER(ctypes.c_int)] * 3),
+    "gms_clear_tune": (_i32, []),
+    "gms_autotune": (_i32, [_i32, _i32, _i64, _vp] + [ctypes.POINTER(ctypes.c_int)] * 3
+                     + [ctypes.POINTER(ctypes.c_double)]),
+    "gms_tune_for": (_i32, [_i32, _i32, _i64] + [ctypes.POINTER(ctypes.c_int)] * 3),
+    "gms_autotune_table": (_i32, [ctypes.c_char_p, _sz, ctypes.POINTER(ctypes.c_size_t)]),
+    "gms_autotune_clear": (_i32, []),
+    "gms_autotune_save": (_i32, [ctypes.c_char_p]),
+    "gms_autotune_load": (_i32, [ctypes.c_char_p]),
     "gms_timing_enable": (_i32, [_i32]),
     "gms_timing_collect": (_i32, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong), _i32]),
     "gms_timing_reset": (_i32, []),
@@ -312,3 +320,42 @@ def sort_host_i32(host_in, host_out, stream=None):
     _check(lib.gms_sort_host_i32(host_in.data_ptr(), host_out.data_ptr(), host_in.numel(), _stream_ptr(stream)),
            "sort_host_i32")
     return host_out
+
+
+def autotune(dtype, n, kv=False, stream=None):
+    """Times the candidate tunings for (dtype, kv, size class of n) on the
+    device and records the fastest; returns {k, sample_b, bulk_copy, ms}."""
+    lib = load()
+    k, b, bulk = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    ms = ctypes.c_double()
+    _check(lib.gms_autotune(DTYPES[dtype], int(bool(kv)), int(n), _stream_ptr(stream), ctypes.byref(k),
+                            ctypes.byref(b), ctypes.byref(bulk), ctypes.byref(ms)), "autotune")
+    return {"k": k.value, "sample_b": b.value, "bulk_copy": bulk.value, "ms": ms.value}
+
+
+def tune_for(dtype, n, kv=False):
+    """The tuning a sort of (dtype, kv, n) would use now."""
+    lib = load()
+    k, b, bulk = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    _check(lib.gms_tune_for(DTYPES[dtype], int(bool(kv)), int(n), ctypes.byref(k), ctypes.byref(b),
+                            ctypes.byref(bulk)), "tune_for")
+    return {"k": k.value, "sample_b": b.value, "bulk_copy": bulk.value}
+
+
+def autotune_table():
+    """The autotuned table as a list of dicts."""
+    import json
+    lib = load()
+    need = ctypes.c_size_t()
+    _check(lib.gms_autotune_table(None, 0, ctypes.byref(need)), "autotune_table")
+    buf = ctypes.create_string_buffer(need.value)
+    _check(lib.gms_autotune_table(buf, need.value, ctypes.byref(need)), "autotune_table")
+    return json.loads(buf.value.decode())
+
+
+def autotune_save(path):
+    _check(load().gms_autotune_save(os.fsencode(path)), "autotune_save")
+
+
+def autotune_load(path):
+    _check(load().gms_autotune_load(os.fsencode(path)), "autotune_load")

@@ -272,11 +272,42 @@ int gms_timing_reset(void);
  *              8 <= sample_b and max_tile/sample_b > k).  A sort whose sample
  *              recursion would get too deep for the tuning returns
  *              GMS_ERR_INVALID.
- *   bulk_copy  1: persistent merge kernel staging segments with cp.async.bulk
- *              (default); 0: one CTA per tile with plain loads
+ *   bulk_copy  1: merge kernel staging each tile's segments in shared memory
+ *              with cp.async.bulk (default); 0: merge with plain loads
+ * A tuning set here applies to every dtype and size until gms_clear_tune,
+ * which returns to the defaults and to the autotuned table below.
  * ------------------------------------------------------------------------- */
 int gms_set_tune(int k, int sample_b, int bulk_copy);
 int gms_get_tune(int* k, int* sample_b, int* bulk_copy);
+int gms_clear_tune(void);
+
+/* ---------------------------------------------------------------------------
+ * Autotuner.  No reference counterpart beyond the sweep scripts named above:
+ * the reference fixes K/PIPELINE/BLOCKS at compile time (src/params.h:18-20).
+ *
+ * gms_autotune times every candidate tuning (k in {8,16,32}, sample_b in
+ * {16,32,64}, both merge paths) on a sort of n synthetic keys of `dtype`
+ * (0 i32, 1 u32, 2 f32, 3 i64, 4 u64, 5 f64; kv=1: with int32 values) on
+ * `stream`, checks that all tunings give the same bits, and records the
+ * fastest (median of repeats) for the size class floor(log2 n).  Later sorts
+ * of that dtype, payload and size class use it unless gms_set_tune is in
+ * force.  Synchronous; allocates its own buffers (about 3 arrays of n keys and
+ * values) and frees them before returning.
+ * gms_tune_for reports the tuning a sort of (dtype, kv, n) would use.
+ * gms_autotune_table writes the table as JSON into buf (needed = bytes with
+ * the terminating NUL; buf may be NULL to query the size).
+ * gms_autotune_save / _load write / read the table as a JSON file recorded
+ * with the GPU's name; a file recorded on another GPU model is refused
+ * (GMS_ERR_INVALID).  If the environment variable GMS_TUNE_CACHE names such a
+ * file, it is loaded before the first sort of the process.
+ * ------------------------------------------------------------------------- */
+int gms_autotune(int dtype, int kv, int64_t n, void* stream, int* out_k, int* out_sample_b, int* out_bulk_copy,
+                 double* out_ms);
+int gms_tune_for(int dtype, int kv, int64_t n, int* k, int* sample_b, int* bulk_copy);
+int gms_autotune_table(char* buf, size_t cap, size_t* needed);
+int gms_autotune_clear(void);
+int gms_autotune_save(const char* path);
+int gms_autotune_load(const char* path);
 
 /* Number of merge rounds (after the base case) a sort of n keys of the given
  * dtype performs, and the base tile (keys) it uses. */

@@ -243,7 +243,7 @@ def test_invalid_arguments(gms):
 
 # ---------------------------------------------------------------------------
 # Tuning: other fan-ins, sample block sizes and both merge paths (bulk-copy
-# persistent merge and one-CTA-per-tile plain loads) must give the same bits.
+# staging and plain loads) must give the same bits.
 TUNES = [(32, 32, 0), (2, 32, 1), (3, 16, 1), (7, 64, 1), (16, 8, 1), (32, 128, 1), (5, 100, 0), (32, 17, 1)]
 
 
@@ -251,7 +251,7 @@ TUNES = [(32, 32, 0), (2, 32, 1), (3, 16, 1), (7, 64, 1), (16, 8, 1), (32, 128, 
 def tuned(gms):
     lib = gms.load()
     yield lib
-    assert lib.gms_set_tune(32, 32, 1) == 0
+    assert lib.gms_clear_tune() == 0
 
 
 @pytest.mark.parametrize("k,b,bulk", TUNES)
