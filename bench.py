@@ -152,6 +152,104 @@ def log_uniform_lengths(rng, lo, hi, total_cap=None, count=None):
     return np.array(out, dtype=np.int64)
 
 
+DIST_NAMES = ["uniform", "sorted", "reverse", "all_equal", "16_values", "zipf_1.2"]
+
+
+def _sort_time(lib, fn, srcs, outs, n, reps, stream):
+    """Median CUDA-event time (ms) of one sort call on a fresh device copy of
+    the inputs per repetition (the copy is outside the events)."""
+    import torch
+
+    work = [t.clone() for t in srcs]
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    times = []
+    with torch.cuda.stream(stream):
+        for r in range(reps + 1):  # the first run warms up
+            for w, t in zip(work, srcs):
+                w.copy_(t)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            if len(srcs) == 1:
+                rc = fn(work[0].data_ptr(), outs[0].data_ptr(), n, 0, sp)
+            else:
+                rc = fn(work[0].data_ptr(), work[1].data_ptr(), outs[0].data_ptr(), outs[1].data_ptr(), n, 0, sp)
+            e1.record(stream)
+            assert rc == 0, lib.gms_last_error()
+            stream.synchronize()
+            if r:
+                times.append(e0.elapsed_time(e1))
+    times.sort()
+    return times[len(times) // 2]
+
+
+def config_sweep(lib, orc, peak, reps=5):
+    """The other sizes, distributions and key/value layouts of the workload
+    set: int32 2^24 uniform; int32 2^28 in the five non-uniform distributions;
+    2^27 uint64 keys + int32 payload and 2^27 float32 keys + int32 payload.
+    Each entry: Gkeys/s (median of `reps`), the fraction of the whole-sort
+    HBM roofline 2*N*bytes_per_element*(1+rounds) at the measured peak, and a
+    bit-exact check against a (stable) torch.sort of the same data."""
+    import numpy as np
+    import torch
+
+    stream = torch.cuda.Stream()
+    out = {}
+
+    def entry(n, ms, elt_bytes, dtype_code, kv, ok):
+        passes = 1 + int(lib.gms_rounds(dtype_code, kv, n))
+        gbs = 2 * n * elt_bytes * passes / (ms * 1e-3) / 1e9
+        return {"n": n, "gkeys_s": round(n / ms / 1e6, 3), "ms": round(ms, 4), "passes": passes,
+                "sort_roofline_frac": round(gbs / peak, 4), "bit_exact": ok}
+
+    # int32, 2^24 uniform and 2^28 in each non-uniform distribution
+    for n, dists in ((1 << 24, [0]), (1 << 28, [1, 2, 3, 4, 5])):
+        for d in dists:
+            src = torch.from_numpy(orc.gen_i32(n, d, SEED)).cuda()
+            dst = torch.empty_like(src)
+            ms = _sort_time(lib, lib.gms_sort_i32, [src], [dst], n, reps, stream)
+            ok = bool(torch.equal(dst, torch.sort(src)[0]))
+            out[f"int32_{DIST_NAMES[d]}_2p{n.bit_length() - 1}"] = entry(n, ms, 4, 0, 0, ok)
+            del src, dst
+            torch.cuda.empty_cache()
+    # key/value: 2^27 uint64 + int32 index, 2^27 float32 + int32 index
+    n = 1 << 27
+    k64 = orc.gen_u64(n, SEED)
+    kf = orc.gen_f32(n, SEED)
+    for name, keys, fn, code, kb in (("uint64_kv_i32_2p27", k64.view(np.int64), lib.gms_sort_kv_u64_i32, 4, 8),
+                                     ("float32_kv_i32_2p27", kf.view(np.int32), lib.gms_sort_kv_f32_i32, 2, 4)):
+        kt = torch.from_numpy(keys).cuda()
+        vt = torch.arange(n, dtype=torch.int32, device="cuda")
+        ko, vo = torch.empty_like(kt), torch.empty_like(vt)
+        ms = _sort_time(lib, fn, [kt, vt], [ko, vo], n, reps, stream)
+        # expected order from a stable torch.sort of order-preserving signed images of the keys
+        if kb == 8:
+            img = kt ^ torch.tensor(-(1 << 63), dtype=torch.int64, device="cuda")
+        else:
+            img = kt ^ ((kt >> 31) & 0x7FFFFFFF)
+        _, idx = torch.sort(img, stable=True)
+        ok = bool(torch.equal(vo, idx.to(torch.int32)) and torch.equal(ko, kt[idx]))
+        del img, idx
+        out[name] = entry(n, ms, kb + 4, code, 1, ok)
+        del kt, vt, ko, vo
+        torch.cuda.empty_cache()
+    return out
+
+
+def library_baselines(n, reps=5):
+    """thrust::sort on the same kind of input: CUB radix sort (keys only) and
+    CUB merge sort (user comparator), from the in-tree thrust_baseline program."""
+    exe = os.path.join(ROOT, "gpu-mms_gb300", "thrust_baseline")
+    if not os.path.exists(exe):
+        return {"unavailable": "thrust_baseline not built"}
+    r = subprocess.run([exe, str(n), str(reps)], capture_output=True, text=True, timeout=600)
+    if r.returncode != 0:
+        return {"unavailable": f"thrust_baseline exited {r.returncode}: {r.stderr.strip()[:200]}"}
+    d = json.loads(r.stdout.strip().splitlines()[-1])
+    d["what"] = "thrust::sort int32 uniform: radix = keys-only (CUB radix sort), merge = user comparator (CUB merge sort)"
+    return d
+
+
 def batched_bench(lib, orc, total_keys, nseg=None, seed=7):
     """Config 4: many int32 arrays, lengths log-uniform in [32, 2^20]; one
     batched (segmented) sort vs its CUDA-graph replay vs one plain call per
@@ -209,7 +307,8 @@ def batched_bench(lib, orc, total_keys, nseg=None, seed=7):
     t_plain = ev_time(lambda: (work.copy_(keys), plain()), 1) - ev_time(lambda: work.copy_(keys), 3)
     same = bool(torch.equal(plain_out, batched_out))
     return {
-        "workload": f"{len(lengths)} int32 arrays, lengths log-uniform in [32, 2^20], {n} keys in all, uniform keys",
+        "workload": f"{len(lengths)} int32 arrays, lengths log-uniform in [32, 2^20], {n} keys in all, uniform keys"
+                    + (f" (the first arrays that fit {total_keys} keys)" if nseg is None else ""),
         "keys": n, "arrays": int(len(lengths)),
         "batched_gkeys_s": round(n / t_batched / 1e6, 3), "batched_ms": round(t_batched, 3),
         "graph_gkeys_s": round(n / t_graph / 1e6, 3), "graph_ms": round(t_graph, 3),
@@ -530,7 +629,9 @@ def run_ours(args):
     if not args.no_extra:
         del inputs
         torch.cuda.empty_cache()
-        line["batched"] = batched_bench(lib, orc, total_keys=1 << 27)
+        line["configs"] = config_sweep(lib, orc, peak)
+        line["library_baselines"] = library_baselines(n)
+        line["batched"] = batched_bench(lib, orc, total_keys=1 << 29)
         line["serving"] = serving_bench(lib, orc, seconds=2.0)
         line["serving_capacity"] = serving_bench(lib, orc, seconds=2.0, rate=0)
         line["serving_small"] = serving_bench(lib, orc, seconds=1.0, rate=20000.0, hi=1 << 16)

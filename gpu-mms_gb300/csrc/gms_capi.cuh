@@ -42,9 +42,17 @@ gms::Tune current_tune();
 gms::Tune tune_for(int dtype, int kv, int64_t n);
 inline gms::Tune default_tune() { return current_tune(); }
 
-// Runs a full sort of one dtype with the scratch cache.
+// Sorts with caller-provided scratch (gms_sort_ws); defined per key width.
+int sort32_ws(int dtype, void* in, void* out, int64_t n, void* ws, size_t ws_bytes, cudaStream_t st);
+int sort64_ws(int dtype, void* in, void* out, int64_t n, void* ws, size_t ws_bytes, cudaStream_t st);
+int sort_kv_ws(int dtype, void* ki, int32_t* vi, void* ko, int32_t* vo, int64_t n, void* ws, size_t ws_bytes,
+               cudaStream_t st);
+
+// Runs a full sort of one dtype, with the scratch cache or, when `user_ws` is
+// given, with the caller's scratch (its status word cleared first).
 template <class Eng, class K, class V>
-int run_sort(K* in, V* vin, K* out, V* vout, int64_t n, cudaStream_t st, int dtype) {
+int run_sort(K* in, V* vin, K* out, V* vout, int64_t n, cudaStream_t st, int dtype, void* user_ws = nullptr,
+             size_t user_bytes = 0) {
   clear_error();
   if (n < 0) return set_error(GMS_ERR_INVALID, "n < 0");
   if (n == 0) return GMS_OK;
@@ -56,8 +64,21 @@ int run_sort(K* in, V* vin, K* out, V* vout, int64_t n, cudaStream_t st, int dty
   if (!l.ok) return set_error(GMS_ERR_INVALID, "tuning too fine for this n (sample recursion too deep)");
   const size_t bytes = gms::ws_bytes_for<K>(l, t.k);
   int status = GMS_OK;
-  void* ws = cache_get(0, bytes, st, &status);
-  if (status != GMS_OK) return status;
+  void* ws = nullptr;
+  if (user_ws) {
+    if (user_bytes < bytes) {
+      char msg[128];
+      snprintf(msg, sizeof(msg), "workspace too small: %zu bytes given, %zu needed", user_bytes, bytes);
+      return set_error(GMS_ERR_INVALID, msg);
+    }
+    if (reinterpret_cast<uintptr_t>(user_ws) % 256) return set_error(GMS_ERR_INVALID, "workspace not 256-byte aligned");
+    cudaError_t e = cudaMemsetAsync(user_ws, 0, 256, st);
+    if (e != cudaSuccess) return cuda_error(e, "workspace status word");
+    ws = user_ws;
+  } else {
+    ws = cache_get(0, bytes, st, &status);
+    if (status != GMS_OK) return status;
+  }
   const gms::WsPtrs<K> w = gms::ws_carve<K>(l, t.k, ws);
   cudaError_t e = Eng::sort(w, in, vin, out, vout, n, t, st);
   if (e != cudaSuccess) return cuda_error(e, "sort");

@@ -17,6 +17,16 @@ int sort32(void* in, void* out, int64_t n, void* st, int dtype) {
 
 }  // namespace
 
+int gms_capi::sort32_ws(int dtype, void* in, void* out, int64_t n, void* ws, size_t bytes, cudaStream_t st) {
+  uint32_t* i = (uint32_t*)in;
+  uint32_t* o = (uint32_t*)out;
+  switch (dtype) {
+    case 0: return run_sort<EngI32, uint32_t, NoVal>(i, nullptr, o, nullptr, n, st, 0, ws, bytes);
+    case 1: return run_sort<EngU32, uint32_t, NoVal>(i, nullptr, o, nullptr, n, st, 1, ws, bytes);
+    default: return run_sort<EngF32, uint32_t, NoVal>(i, nullptr, o, nullptr, n, st, 2, ws, bytes);
+  }
+}
+
 extern "C" {
 
 int gms_sort_i32(int32_t* in, int32_t* out, int64_t n, int tb, void* st) {

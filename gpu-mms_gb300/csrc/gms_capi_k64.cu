@@ -17,6 +17,16 @@ int sort64(void* in, void* out, int64_t n, void* st, int dtype) {
 
 }  // namespace
 
+int gms_capi::sort64_ws(int dtype, void* in, void* out, int64_t n, void* ws, size_t bytes, cudaStream_t st) {
+  uint64_t* i = (uint64_t*)in;
+  uint64_t* o = (uint64_t*)out;
+  switch (dtype) {
+    case 3: return run_sort<EngI64, uint64_t, NoVal>(i, nullptr, o, nullptr, n, st, 3, ws, bytes);
+    case 4: return run_sort<EngU64, uint64_t, NoVal>(i, nullptr, o, nullptr, n, st, 4, ws, bytes);
+    default: return run_sort<EngF64, uint64_t, NoVal>(i, nullptr, o, nullptr, n, st, 5, ws, bytes);
+  }
+}
+
 extern "C" {
 
 int gms_sort_i64(int64_t* in, int64_t* out, int64_t n, int tb, void* st) {

@@ -12,6 +12,25 @@ int kv(void* ki, int32_t* vi, void* ko, int32_t* vo, int64_t n, void* st, int dt
 
 }  // namespace
 
+int gms_capi::sort_kv_ws(int dtype, void* ki, int32_t* vi, void* ko, int32_t* vo, int64_t n, void* ws, size_t bytes,
+                         cudaStream_t st) {
+  uint32_t *i4 = (uint32_t*)ki, *o4 = (uint32_t*)ko;
+  uint64_t *i8 = (uint64_t*)ki, *o8 = (uint64_t*)ko;
+  switch (dtype) {
+    case 0: return run_sort<KvEngine<uint32_t, gms::SignFlip32>, uint32_t, int32_t>(i4, vi, o4, vo, n, st, 0, ws, bytes);
+    case 1:
+      return run_sort<KvEngine<uint32_t, gms::IdentityCodec<uint32_t>>, uint32_t, int32_t>(i4, vi, o4, vo, n, st, 1, ws,
+                                                                                          bytes);
+    case 2: return run_sort<KvEngine<uint32_t, gms::FloatOrder32>, uint32_t, int32_t>(i4, vi, o4, vo, n, st, 2, ws, bytes);
+    case 3: return run_sort<KvEngine<uint64_t, gms::SignFlip64>, uint64_t, int32_t>(i8, vi, o8, vo, n, st, 3, ws, bytes);
+    case 4:
+      return run_sort<KvEngine<uint64_t, gms::IdentityCodec<uint64_t>>, uint64_t, int32_t>(i8, vi, o8, vo, n, st, 4, ws,
+                                                                                          bytes);
+    default:
+      return run_sort<KvEngine<uint64_t, gms::FloatOrder64>, uint64_t, int32_t>(i8, vi, o8, vo, n, st, 5, ws, bytes);
+  }
+}
+
 extern "C" {
 
 int gms_sort_kv_i32_i32(int32_t* ki, int32_t* vi, int32_t* ko, int32_t* vo, int64_t n, int tb, void* st) {

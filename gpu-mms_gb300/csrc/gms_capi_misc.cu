@@ -255,6 +255,31 @@ int gms_device_status(void* stream, int* status_out) {
   return GMS_OK;
 }
 
+int gms_sort_ws(int dtype, int kv, void* keys_in, int32_t* vals_in, void* keys_out, int32_t* vals_out, int64_t n,
+                void* workspace, size_t workspace_bytes, void* stream) {
+  clear_error();
+  if (dtype < 0 || dtype > 5 || (kv != 0 && kv != 1)) return set_error(GMS_ERR_INVALID, "dtype in 0..5, kv 0 or 1");
+  if (!workspace) return set_error(GMS_ERR_INVALID, "null workspace");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (kv) return sort_kv_ws(dtype, keys_in, vals_in, keys_out, vals_out, n, workspace, workspace_bytes, st);
+  if (dtype < 3) return sort32_ws(dtype, keys_in, keys_out, n, workspace, workspace_bytes, st);
+  return sort64_ws(dtype, keys_in, keys_out, n, workspace, workspace_bytes, st);
+}
+
+int gms_workspace_status(void* workspace, void* stream, int* status_out) {
+  clear_error();
+  if (!workspace || !status_out) return set_error(GMS_ERR_INVALID, "null pointer");
+  *status_out = 0;
+  cudaStream_t st = (cudaStream_t)stream;
+  int v = 0;
+  cudaError_t e = cudaMemcpyAsync(&v, workspace, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(workspace, 0, sizeof(int), st);
+  if (e != cudaSuccess) return cuda_error(e, "workspace status word");
+  *status_out = v;
+  return GMS_OK;
+}
+
 int gms_reserve(int dtype, int kv, int64_t n, void* stream) {
   clear_error();
   if (dtype < 0 || dtype > GMS_RESERVE_SEGMENTED_I32 || n < 0) return set_error(GMS_ERR_INVALID, "bad dtype or n");

@@ -25,6 +25,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgms.so")
 CLI = os.path.join(HERE, "testmm")
+THRUST = os.path.join(HERE, "thrust_baseline")
 INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -87,10 +88,21 @@ def build(force=False, jobs=None, verbose=False):
             raise RuntimeError(f"nvcc failed for testmm:\n{r.stdout}\n{r.stderr}")
         os.replace(CLI + ".tmp", CLI)
 
-    with ThreadPoolExecutor(max_workers=jobs or len(UNITS) + 1) as ex:
+    def compile_thrust():
+        # thrust_baseline: GPU library baselines (CUB radix and merge sort via thrust)
+        cmd = [nvcc] + ARCH + ["-O2", "-std=c++17", "--extended-lambda",
+                               os.path.join(HERE, "cli", "thrust_baseline.cu"), "-o", THRUST + ".tmp"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed for thrust_baseline:\n{r.stdout}\n{r.stderr}")
+        os.replace(THRUST + ".tmp", THRUST)
+
+    with ThreadPoolExecutor(max_workers=jobs or len(UNITS) + 2) as ex:
         cli = ex.submit(compile_cli)
+        thr = ex.submit(compile_thrust)
         objs = list(ex.map(compile_one, UNITS))
         cli.result()
+        thr.result()
     tmp = LIB + ".tmp"
     cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -146,6 +158,8 @@ SIGNATURES = {
     "gms_reserve": (_i32, [_i32, _i32, _i64, _vp]),
     "gms_device_status": (_i32, [_vp, ctypes.POINTER(ctypes.c_int)]),
     "gms_release_workspaces": (None, []),
+    "gms_sort_ws": (_i32, [_i32, _i32, _vp, _vp, _vp, _vp, _i64, _vp, _sz, _vp]),
+    "gms_workspace_status": (_i32, [_vp, _vp, ctypes.POINTER(ctypes.c_int)]),
     "gms_launch_count": (ctypes.c_longlong, []),
     "gms_set_tune": (_i32, [_i32, _i32, _i32]),
     "gms_get_tune": (_i32, [ctypes.POINTER(ctypes.c_int)] * 3),

@@ -240,6 +240,21 @@ size_t gms_workspace_bytes(int dtype, int kv, int64_t n);
 int gms_reserve(int dtype, int kv, int64_t n, void* stream);
 void gms_release_workspaces(void);
 
+/* Explicit workspace (for serving layers that own their memory): one sort of
+ * `dtype`/`kv` (codes above; vals NULL when kv = 0) that uses `workspace`, a
+ * 256-byte-aligned device buffer of at least gms_workspace_bytes(dtype, kv, n)
+ * bytes (query it after any gms_set_tune / gms_autotune that could change the
+ * tuning of this size), instead of the per-stream cache: the call allocates
+ * nothing.  Its first 256 bytes are the status word of this workspace, cleared
+ * by the call; gms_workspace_status reads (and clears) it like
+ * gms_device_status.  A too-small or misaligned workspace is GMS_ERR_INVALID.
+ * Calls sharing one workspace must be ordered (one stream).
+ * Replaces the reference's per-call cudaMalloc/cudaFree of its pivot array
+ * (src/multimergesort.hxx:62,138). */
+int gms_sort_ws(int dtype, int kv, void* keys_in, int32_t* vals_in, void* keys_out, int32_t* vals_out, int64_t n,
+                void* workspace, size_t workspace_bytes, void* stream);
+int gms_workspace_status(void* workspace, void* stream, int* status_out);
+
 /* Waits for `stream`, then reads and clears the device status word of the
  * stream's scratch: 0 = no kernel reported a problem; bit 0 = a tile exceeded
  * the shared-memory capacity and was skipped; bit 1 = a tile boundary lay

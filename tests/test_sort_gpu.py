@@ -276,3 +276,46 @@ def test_tune_rejects_bad_values(gms, tuned):
     assert lib.gms_set_tune(33, 32, 1) == 1
     assert lib.gms_set_tune(32, 0, 1) == 1
     assert lib.gms_set_tune(32, 300, 1) == 1  # 8704/300 - 32 < 1
+
+
+# Explicit workspace: same bits as the cached-scratch sort, for keys-only and
+# key/value dtypes; too-small and misaligned workspaces are refused.
+@pytest.mark.parametrize("dtype,kv", [(0, 0), (2, 0), (4, 0), (5, 0), (0, 1), (4, 1), (2, 1)])
+def test_sort_with_explicit_workspace(gms, oracle, dtype, kv):
+    lib = gms.load()
+    n = 1_234_567
+    np_t = {0: np.int32, 2: np.float32, 4: np.uint64, 5: np.float64}[dtype]
+    if dtype == 0:
+        keys = oracle.gen_i32(n, 6, 5)
+    elif dtype == 2:
+        keys = oracle.gen_f32(n, 5)
+    elif dtype == 4:
+        keys = oracle.gen_u64(n, 5)
+        keys[::3] = keys[1]
+    else:
+        keys = oracle.gen_f32(n, 6).astype(np.float64)
+    vals = np.arange(n, dtype=np.int32)
+    view = np.int64 if keys.itemsize == 8 else np.int32
+    kin = torch.from_numpy(keys.view(view).copy()).cuda()
+    kout = torch.empty_like(kin)
+    vin = torch.from_numpy(vals).cuda() if kv else None
+    vout = torch.empty_like(vin) if kv else None
+    need = lib.gms_workspace_bytes(dtype, kv, n)
+    assert need > 0
+    ws = torch.empty(need + 256, dtype=torch.uint8, device="cuda")
+    base = ws.data_ptr() + (-ws.data_ptr()) % 256
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    vp = lambda t: t.data_ptr() if t is not None else None  # noqa: E731
+    assert lib.gms_sort_ws(dtype, kv, kin.data_ptr(), vp(vin), kout.data_ptr(), vp(vout), n, base, need - 8, st) == 1
+    assert lib.gms_sort_ws(dtype, kv, kin.data_ptr(), vp(vin), kout.data_ptr(), vp(vout), n, base + 8, need, st) == 1
+    rc = lib.gms_sort_ws(dtype, kv, kin.data_ptr(), vp(vin), kout.data_ptr(), vp(vout), n, base, need, st)
+    assert rc == 0, lib.gms_last_error()
+    flag = ctypes.c_int(-1)
+    assert lib.gms_workspace_status(base, st, ctypes.byref(flag)) == 0 and flag.value == 0
+    got = kout.cpu().numpy().view(np_t)
+    if kv:
+        wk, wv = oracle.sort_kv(keys, vals)
+        assert np.array_equal(got.view(np.uint8), wk.view(np.uint8))
+        assert np.array_equal(vout.cpu().numpy(), wv)
+    else:
+        assert np.array_equal(got.view(np.uint8), oracle.sort(keys).view(np.uint8))
