@@ -24,6 +24,36 @@ struct Rec {
 };
 __forceinline__ __device__ int rec_cmp(Rec a, Rec b) { return a.key < b.key; }
 
+// A packed 32-bit key + 32-bit value in the shape of the reference's
+// commented testType (cmp.hxx:59-73): the cast to and assignments from a
+// 64-bit CASTTYPE word that its warp shuffles need.  This build never shuffles
+// keys, but such a type must still compile and sort (by key, stably).
+struct PackedKV {
+  int key;
+  int val;
+  __forceinline__ __device__ operator long long() const {
+    return (long long)(unsigned)key + (long long)((unsigned long long)(unsigned)val << 32);
+  }
+  __forceinline__ __device__ PackedKV& operator=(const long long& w) {
+    key = (int)w;
+    val = (int)(w >> 32);
+    return *this;
+  }
+};
+__forceinline__ __device__ int packed_cmp(PackedKV a, PackedKV b) { return a.key < b.key; }
+
+// The reference's alternative comparator examples on a 64-bit word
+// (cmp.hxx:41-46): the low 32 bits as a signed int ("L1-norm"), and a
+// fraction numerator/denominator packed high/low, compared exactly by
+// cross-multiplication (denominators positive).
+__forceinline__ __device__ int low32_cmp(long long a, long long b) { return (int)a < (int)b; }
+__forceinline__ __device__ int frac_cmp(long long a, long long b) {
+  return (long long)(int)(a >> 32) * (int)b < (long long)(int)(b >> 32) * (int)a;
+}
+static bool host_frac_less(long long a, long long b) {
+  return (long long)(int)(a >> 32) * (int)b < (long long)(int)(b >> 32) * (int)a;
+}
+
 static int failures = 0;
 
 template <class T, int (*f)(T, T), class HostLess>
@@ -62,6 +92,19 @@ int main() {
     for (int i = 0; i < n; ++i) r[i] = Rec{(int)(g() % 97), i};
     run_case<Rec, rec_cmp>("key/value record (stable)", r, [](const Rec& x, const Rec& y) { return x.key < y.key; },
                            false);
+    std::vector<PackedKV> pk(n);
+    for (int i = 0; i < n; ++i) pk[i] = PackedKV{(int)(g() % 301) - 150, i};
+    run_case<PackedKV, packed_cmp>("packed testType (stable)", pk,
+                                   [](const PackedKV& x, const PackedKV& y) { return x.key < y.key; }, true);
+    std::vector<long long> w(n);
+    for (int i = 0; i < n; ++i) {
+      const long long num = (long long)(g() % 2001) - 1000, den = 1 + (long long)(g() % 64);
+      w[i] = (long long)((unsigned long long)num << 32) | (unsigned long long)den;
+    }
+    run_case<long long, frac_cmp>("fraction num/den (stable)", w, host_frac_less, false);
+    for (int i = 0; i < n; ++i) w[i] = (long long)(((unsigned long long)g() << 32) | g());
+    run_case<long long, low32_cmp>("low 32 bits as int (stable)", w,
+                                   [](long long x, long long y) { return (int)x < (int)y; }, false);
   }
   // the full key range: MAXVAL is an ordinary key here
   std::vector<int> ext(100003);

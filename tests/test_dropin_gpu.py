@@ -1,7 +1,8 @@
 """The header-only drop-in (include/multimergesort.hxx) compiled into a caller
 written for GPU-MMS's multimergesort<T,cmp>: default, descending, absolute
-value and packed key/value comparators, 4- and 5-argument forms, checked
-against std::stable_sort on the host (tests/dropin/dropin_main.cu)."""
+value, packed key/value records (including the CASTTYPE-cast testType shape),
+fraction and low-32-bit comparators on 64-bit words, 4- and 5-argument forms,
+checked against std::stable_sort on the host (tests/dropin/dropin_main.cu)."""
 import os
 import subprocess
 
