@@ -454,16 +454,28 @@ struct MergeSmemLayout {
   static constexpr size_t off_mk = off_stage_v + stage_v_bytes;
   static constexpr size_t off_mv = off_mk + mk_bytes;
   static constexpr size_t off_desc = off_mv + mv_bytes;
-  // cpre[33] int, sbk[32] int, sbv[32] int, (pad), gsrc[32] int64, meta[4] int64, bar
+  // cpre[33] int, sbk[32] int, sbv[32] int, (pad), gsrc[32] int64, meta[4] int64, bar,
+  // wst[kLevels][17] int (first thread of each pair's windows, per level)
+  static constexpr int kLevels = 5;  // log2(kMaxK)
   static constexpr size_t off_gsrc = off_desc + 4 * (33 + 32 + 32) + 4;
   static constexpr size_t off_meta = off_gsrc + 8 * 32;
   static constexpr size_t off_bar = off_meta + 8 * 4;
-  static constexpr size_t bytes = off_bar + 16;
+  static constexpr size_t off_wst = off_bar + 16;
+  static constexpr size_t bytes = off_wst + 4 * kLevels * 17;
+};
+
+// Merge-tile capacity with window-aligned levels: at a level with np pairs
+// the windows of ITEMS outputs that never cross a pair end number at most
+// cnt/ITEMS + np, which fits NT threads when cnt <= (NT - kMaxK/2) * ITEMS.
+template <int NT, int ITEMS>
+struct WindowCap {
+  static constexpr int value = (NT - 16) * ITEMS;
 };
 
 template <class KeyT, class V, class Cmp, class Codec, int NT, int ITEMS>
 __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, int64_t total_tiles) {
-  constexpr int CAP = NT * ITEMS;
+  constexpr int CAP = NT * ITEMS;                        // shared-memory buffers
+  constexpr int TILE_MAX = WindowCap<NT, ITEMS>::value;  // keys a tile may hold
   constexpr bool kHasVal = HasVal<V>::value;
   using Lay = MergeSmemLayout<KeyT, V, CAP>;
   static_assert(Lay::off_gsrc % 8 == 0, "descriptor alignment");
@@ -480,6 +492,7 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
   int64_t* gsrc = reinterpret_cast<int64_t*>(smem + Lay::off_gsrc);
   int64_t* meta = reinterpret_cast<int64_t*>(smem + Lay::off_meta);
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem + Lay::off_bar);
+  int* wst = reinterpret_cast<int*>(smem + Lay::off_wst);
   const Cmp cmp;
   const int tid = threadIdx.x;
   const int lane = tid & 31;
@@ -510,7 +523,7 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
       const int64_t lo = a.desc[row * nk + lane];
       const int64_t hi = a.desc[(row + 1) * nk + lane];
       const int64_t rl = min64(a.L, ng - min64((int64_t)lane * a.L, ng));
-      bad = !((lo >= 0) && (hi >= lo) && (hi <= rl) && (hi - lo <= CAP));
+      bad = !((lo >= 0) && (hi >= lo) && (hi <= rl) && (hi - lo <= TILE_MAX));
       len = bad ? 0 : (int)(hi - lo);
       gs = gbase + (int64_t)lane * a.L + (bad ? 0 : lo);
     }
@@ -521,9 +534,29 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
       if (lane >= o) incl += y;
     }
     const int total = __shfl_sync(0xffffffffu, incl, 31);
-    const bool any_bad = __any_sync(0xffffffffu, bad) || total > CAP;
+    const bool any_bad = __any_sync(0xffffffffu, bad) || total > TILE_MAX;
     if (lane < nk) cpre[lane + 1] = incl;
     if (lane == 0) cpre[0] = 0;
+    // window table of every level: pair p of a level with `span` segments
+    // holds keys [cpre[p*span], cpre[min(p*span+span, nk)]) and gets
+    // ceil(len/ITEMS) threads starting at wst[lev*17 + p]
+    for (int lev = 0, span = 2; lev < Lay::kLevels && (lev == 0 || (span >> 1) < nk); ++lev, span <<= 1) {
+      const int np = (nk + span - 1) / span;
+      const int si = lane * span;
+      const int ei = min(si + span, nk);
+      const int ps = __shfl_sync(0xffffffffu, incl, max(min(si, nk) - 1, 0));
+      const int pe = __shfl_sync(0xffffffffu, incl, max(ei - 1, 0));
+      const int len = (lane < np) ? (si == 0 ? pe : pe - ps) : 0;
+      const int tcount = (len + ITEMS - 1) / ITEMS;
+      int tincl = tcount;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, tincl, o);
+        if (lane >= o) tincl += y;
+      }
+      if (lane < np) wst[lev * 17 + lane + 1] = tincl;
+      if (lane == 0) wst[lev * 17] = 0;
+    }
     // key regions
     const uint64_t A = arr_k_lo + (uint64_t)gs * sizeof(KeyT);
     const uint64_t E = A + (uint64_t)len * sizeof(KeyT);
@@ -636,52 +669,59 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
   const int64_t out_base = meta[0];
   const int64_t run_base = meta[1];
   const int64_t run_index = meta[2];
-  const int s = tid * ITEMS;
 
-  // ---- level 1: staged segment pairs -> merge buffer ----
-  if (s < cnt) {
-    const int npairs = (nk + 1) / 2;
-    const EncLoad<KeyT, Codec> ld(reinterpret_cast<const KeyT*>(stage_k), a.enc_on_load);
-    auto pair_of = [&](int q) -> PairRange {
-      const int p = find_pair(cpre, npairs, 2, q);
-      const int ka_ = 2 * p;
-      const int kb_ = min(2 * p + 1, nk);
-      const int na = cpre[ka_ + 1] - cpre[ka_];
-      const int nb = (kb_ < nk) ? cpre[kb_ + 1] - cpre[kb_] : 0;
-      const int a0 = sbk[ka_];
-      const int b0 = (kb_ < nk) ? sbk[kb_] : a0 + na;
-      return PairRange{cpre[ka_], a0, a0 + na, b0, b0 + nb, p};
-    };
-    const SmemArray<KeyT> yka(k1 + s);
-    const SmemArray<V> yva(v1 + s);
-    const SmemArray<V> sva(reinterpret_cast<const V*>(stage_v));
-    const int gen = a.gen_index;
-    merge_thread<ITEMS, KeyT>(s, ld, cmp, pair_of, [&](int i, KeyT k, uint32_t src, bool ta, const PairRange& P) {
-      yka.put(i, k);
-      if constexpr (kHasVal) {
-        const int seg = ta ? 2 * P.id : 2 * P.id + 1;
-        const int off = (int)((src - ld.base) / (uint32_t)sizeof(KeyT)) - sbk[seg];
-        yva.put(i, gen ? (V)(gsrc[seg] + off) : sva.get(sbv[seg] + off));
+  // ---- levels: window-aligned merges, pair by pair ----
+  // Level 0 merges staged segment pairs (2p, 2p+1) into the merge buffer; the
+  // later levels ping-pong between the merge buffer and the staging buffer,
+  // pair p of level `lev` merging the outputs of pairs 2p and 2p+1 below.
+  int cur = 0;  // 0: the staging buffer holds the current input
+  for (int lev = 0, span = 2; lev == 0 || (span >> 1) < nk; ++lev, span <<= 1) {
+    const int np = (nk + span - 1) / span;
+    const int* wt = wst + lev * 17;
+    if (tid < wt[np]) {
+      int p = 0;  // the last pair whose first window thread is <= tid
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1) {
+        if (p + step < np && wt[p + step] <= tid) p += step;
       }
-    });
-  }
-  __syncthreads();
-  int cur = 1;
-  // ---- remaining levels: merge buffer <-> staging buffer ----
-  for (int span = 4; span < 2 * nk; span *= 2) {
-    const KeyT* xk = (cur ? k1 : k0);
-    KeyT* yk = (cur ? k0 : k1);
-    const V* xv = (cur ? v1 : v0);
-    V* yv = (cur ? v0 : v1);
-    if (s < cnt) {
-      const PlainLoad<KeyT> ld(xk);
-      const SmemArray<KeyT> yka(yk + s);
-      const SmemArray<V> xva(xv), yva(yv + s);
-      const CompactPairs pairs{cpre, nk, span, (nk + span - 1) >> (31 - __clz(span))};
-      merge_thread<ITEMS, KeyT>(s, ld, cmp, pairs, [&](int i, KeyT k, uint32_t src, bool, const PairRange&) {
-        yka.put(i, k);
-        if constexpr (kHasVal) yva.put(i, xva.get((int)((src - ld.base) / (uint32_t)sizeof(KeyT))));
-      });
+      const int si = p * span;
+      const int mi = min(si + (span >> 1), nk);
+      const int ei = min(si + span, nk);
+      const int ps = cpre[si], pm = cpre[mi], pe = cpre[ei];
+      const int diag = (tid - wt[p]) * ITEMS;
+      const int m = min(ITEMS, pe - ps - diag);
+      const int na = pm - ps, nb = pe - pm;
+      if (lev == 0) {
+        const EncLoad<KeyT, Codec> ld(reinterpret_cast<const KeyT*>(stage_k), a.enc_on_load);
+        const uint32_t A0 = ld.addr(sbk[si]);
+        const uint32_t B0 = (si + 1 < nk) ? ld.addr(sbk[si + 1]) : A0 + (uint32_t)na * sizeof(KeyT);
+        const SmemArray<KeyT> yka(k1 + ps + diag);
+        const SmemArray<V> yva(v1 + ps + diag);
+        const SmemArray<V> sva(reinterpret_cast<const V*>(stage_v));
+        const int gen = a.gen_index;
+        merge_window<ITEMS, KeyT>(ld, cmp, A0, na, B0, nb, diag, m, [&](int i, KeyT k, uint32_t src, bool ta) {
+          yka.put(i, k);
+          if constexpr (kHasVal) {
+            const int seg = ta ? si : si + 1;
+            const int off = (int)((src - ld.base) / (uint32_t)sizeof(KeyT)) - sbk[seg];
+            yva.put(i, gen ? (V)(gsrc[seg] + off) : sva.get(sbv[seg] + off));
+          }
+        });
+      } else {
+        const KeyT* xk = (cur ? k1 : k0);
+        KeyT* yk = (cur ? k0 : k1);
+        const V* xv = (cur ? v1 : v0);
+        V* yv = (cur ? v0 : v1);
+        const PlainLoad<KeyT> ld(xk);
+        const SmemArray<KeyT> yka(yk + ps + diag);
+        const SmemArray<V> xva(xv), yva(yv + ps + diag);
+        merge_window<ITEMS, KeyT>(ld, cmp, ld.addr(ps), na, ld.addr(pm), nb, diag, m,
+                                  [&](int i, KeyT k, uint32_t src, bool) {
+                                    yka.put(i, k);
+                                    if constexpr (kHasVal)
+                                      yva.put(i, xva.get((int)((src - ld.base) / (uint32_t)sizeof(KeyT))));
+                                  });
+      }
     }
     __syncthreads();
     cur ^= 1;

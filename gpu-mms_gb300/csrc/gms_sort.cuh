@@ -193,6 +193,8 @@ struct Engine {
   // base-case tile (NT threads x ITEMS keys) and merge tile (NTM x ITEMSM)
   static constexpr int CAP = NT * ITEMS;
   static constexpr int CAPM = NTM * ITEMSM;
+  // largest forecast tile: the merge kernel's window-aligned capacity
+  static constexpr int CAPW = WindowCap<NTM, ITEMSM>::value;
   // Keys-only sorts of 4- and 8-byte integer keys use the warp-shuffle base
   // case: 256 x 32 keys (4-byte) or 512 x 16 keys (8-byte), 8192-key tiles.
   static constexpr bool kWarpBase =
@@ -219,7 +221,7 @@ struct Engine {
       return;
     }
     const int sb = t.sample_b;
-    const int64_t G = CAPM / sb - k;
+    const int64_t G = CAPW / sb - k;
     const int64_t runs = ceil_div(n, L);
     const int64_t Ls = ceil_div(L, sb);
     const int64_t ns = (runs - 1) * Ls + ceil_div(n - (runs - 1) * L, sb);
@@ -343,7 +345,7 @@ struct Engine {
       return launch_tile<MODE_GROUP>(a, groups, st, level);
     }
     if (level + 1 >= kMaxLevels) return cudaErrorInvalidValue;
-    const int64_t G = CAPM / sb - k;
+    const int64_t G = CAPW / sb - k;
     const int64_t runs = ceil_div(n, L);
     const int64_t Ls = ceil_div(L, sb);
     const int64_t ns = (runs - 1) * Ls + ceil_div(n - (runs - 1) * L, sb);

@@ -73,6 +73,9 @@ inline void* scratch(size_t bytes, cudaError_t* err) {
 template <typename T, int (*f)(T, T)>
 T* run(T* input, T* output, int N) {
   using Eng = DropinEngine<T, f>;
+  static_assert(GMS_K >= 2 && GMS_K <= 32, "GMS_K (fan-in) must be in [2, 32]");
+  static_assert(GMS_SAMPLE_B >= 8 && Eng::CAPW / GMS_SAMPLE_B - GMS_K >= 1,
+                "GMS_SAMPLE_B must be >= 8 and leave room for a merge tile");
   if (N < 0 || (N > 0 && (!input || !output))) {
     last_error_slot() = "multimergesort: bad arguments";
     fprintf(stderr, "%s\n", last_error_slot());

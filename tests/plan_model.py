@@ -15,13 +15,37 @@ def ceil_div(a, b):
 
 
 class Geometry:
-    """cap: merge-tile capacity; base: base-case tile (defaults to cap)."""
+    """cap: one-CTA group capacity (GROUP mode when K*L <= cap); base:
+    base-case tile (defaults to cap).  With nt/items (the merge kernel's
+    threads and keys per thread) forecast tiles are cut for the window-aligned
+    capacity (nt - 16) * items (WindowCap in gms_kernels.cuh), and every tile
+    is checked to need at most nt windows at every merge level; without them
+    tiles are cut for cap."""
 
-    def __init__(self, cap, k, b, base=None):
+    def __init__(self, cap, k, b, base=None, nt=None, items=None):
         self.cap, self.k, self.b = cap, k, b
         self.base = base or cap
-        self.g = cap // b - k
-        assert self.g > 0, "tile geometry needs CAP/B > K"
+        self.nt, self.items = nt, items
+        self.tile_cap = (nt - 16) * items if nt else cap
+        self.g = self.tile_cap // b - k
+        assert self.g > 0, "tile geometry needs TILE_CAP/B > K"
+
+
+def windows_per_level(seg_lens, items):
+    """Threads the window-aligned merge levels of one tile use: at the level
+    with `span` segments per pair, sum over pairs of ceil(len / items)."""
+    k = len(seg_lens)
+    out = []
+    span = 2
+    while True:
+        tot = 0
+        for p in range(0, k, span):
+            tot += ceil_div(int(sum(seg_lens[p:p + span])), items)
+        out.append(tot)
+        if span >= k:
+            break
+        span *= 2
+    return out
 
 
 def _stable_merge(keys, idx):
@@ -113,8 +137,12 @@ def model_round(keys, idx, L, geo, stats, level=0):
             ti = np.concatenate(seg_i)
             cnt = len(tk)
             max_tile = max(max_tile, cnt)
-            assert cnt <= cap, f"tile of {cnt} keys exceeds CAP={cap} (level {level})"
+            assert cnt <= geo.tile_cap, f"tile of {cnt} keys exceeds {geo.tile_cap} (level {level})"
             assert cnt <= (G + k) * B
+            if geo.nt:
+                w = windows_per_level([len(x) for x in seg_k], geo.items)
+                assert max(w) <= geo.nt, f"tile needs {max(w)} window threads > {geo.nt}"
+                stats["max_windows"] = max(stats.get("max_windows", 0), max(w))
             mk, mi = _stable_merge(tk, ti)
             o = gbase + doff[j]
             out_k[o:o + cnt] = mk

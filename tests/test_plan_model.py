@@ -32,21 +32,28 @@ def test_tiles_fit_and_sort_is_stable(cap, k, b):
 
 @pytest.mark.parametrize("base", [8704, 8192])
 def test_production_geometry_one_round(base):
-    """Merge tiles of 8704 keys; base tiles of 8704 (key/value) or 8192
-    (keys-only warp base case)."""
-    geo = Geometry(8704, 32, 32, base=base)
+    """The merge kernel's geometry (512 threads x 17 keys: forecast tiles of at
+    most 8432 keys, window-aligned levels within 512 threads); base tiles of
+    8704 (key/value) or 8192 (keys-only warp base case)."""
+    geo = Geometry(8704, 32, 32, base=base, nt=512, items=17)
     rng = np.random.default_rng(0)
     for name, x in dists(rng, base * 32 + 4321):
         sk, si, st = model_sort(x.astype(np.int64), geo)
         assert np.array_equal(si, np.argsort(x, kind="stable")), name
         for _, m in st.get("max_tile", []):
-            assert m <= 8704
+            assert m <= 8432
+        assert st["max_windows"] <= 512
 
 
-def test_base_smaller_than_merge_tile_deep():
-    geo = Geometry(96, 4, 4, base=64)
-    rng = np.random.default_rng(5)
-    for n in [65, 256, 257, 1025, 5000]:
+@pytest.mark.parametrize("k,b", [(2, 2), (3, 2), (4, 4), (8, 2), (16, 2), (32, 2)])
+def test_window_threads_fit_small_geometry(k, b):
+    """Window-aligned levels on a small geometry (nt=48, items=5: forecast
+    tiles of at most 160 keys, groups of 240) across fan-ins, skewed inputs
+    included: every tile's levels fit the 48 threads."""
+    geo = Geometry(240, k, b, base=16, nt=48, items=5)
+    rng = np.random.default_rng(k * 100 + b)
+    for n in [17, 300, 2000]:
         for name, x in dists(rng, n):
             sk, si, st = model_sort(x.astype(np.int64), geo)
             assert np.array_equal(si, np.argsort(x, kind="stable")), (n, name)
+            assert st.get("max_windows", 0) <= 48
