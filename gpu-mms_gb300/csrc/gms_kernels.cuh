@@ -342,18 +342,21 @@ template <int NT, int KPL, int ITEMS_M>
 struct BaseWarpGeom {
   static constexpr int TILE = NT * KPL;
   static constexpr int WARP_RUN = 32 * KPL;
-  static constexpr int MERGE_THREADS = (TILE + ITEMS_M - 1) / ITEMS_M;
-  static_assert(MERGE_THREADS <= NT, "merge phase needs TILE <= NT*ITEMS_M");
+  static constexpr int log2i(int x) { return x <= 1 ? 0 : 1 + log2i(x / 2); }
+  static constexpr int LEVELS = log2i(TILE / WARP_RUN);  // shared-memory merge levels
+  static_assert((WARP_RUN << LEVELS) == TILE, "TILE must be WARP_RUN times a power of two");
+  // the windows of the first level (pairs of WARP_RUN keys) must fit the block
+  static constexpr int WINDOWS = (TILE / (2 * WARP_RUN)) * ((2 * WARP_RUN + ITEMS_M - 1) / ITEMS_M);
+  static_assert(LEVELS == 0 || WINDOWS <= NT, "merge windows exceed the block");
   static_assert((KPL & (KPL - 1)) == 0 && KPL % 4 == 0, "KPL must be a power of two, multiple of 4");
 };
 
-// Each ping-pong buffer covers every position a merge thread emits
-// (MERGE_THREADS*ITEMS_M, which can exceed TILE) plus slack for the cursor's
-// look-past load.
+// Each ping-pong buffer holds the tile plus slack for the reads past a pair's
+// end of the last window of a pair (at most ITEMS_M/2 + 2 keys).
 template <class KeyT, int NT, int KPL, int ITEMS_M>
 struct BaseWarpSmem {
   using Geo = BaseWarpGeom<NT, KPL, ITEMS_M>;
-  static constexpr int SPAN = Geo::MERGE_THREADS * ITEMS_M > Geo::TILE ? Geo::MERGE_THREADS * ITEMS_M : Geo::TILE;
+  static constexpr int SPAN = Geo::TILE + ITEMS_M;
   static constexpr size_t buf = ((sizeof(KeyT) * (SPAN + 4) + 15) / 16) * 16;
   static constexpr size_t bytes = 2 * buf;
 };
@@ -404,18 +407,24 @@ __global__ void __launch_bounds__(NT) base_warp_kernel(TileArgs<KeyT, NoVal> a) 
     for (int r = 0; r < KPL; ++r) dst.put(r, x[r]);
   }
   __syncthreads();
-  // shared-memory merge levels: runs of WARP_RUN ... TILE/2
+  // shared-memory merge levels: runs of WARP_RUN ... TILE/2.  Each pair of a
+  // level gets ceil(2*rl/ITEMS_M) threads whose windows never cross its end.
   int cur = 0;
-  const int s = tid * ITEMS_M;
-  for (int rl = Geo::WARP_RUN; rl < TILE; rl *= 2) {
+#pragma unroll
+  for (int lv = 0; lv < Geo::LEVELS; ++lv) {
+    const int rl = Geo::WARP_RUN << lv;
+    const int tpp = (2 * rl + ITEMS_M - 1) / ITEMS_M;
     const KeyT* xk = cur ? k1 : k0;
     KeyT* yk = cur ? k0 : k1;
-    if (tid < Geo::MERGE_THREADS) {
+    if (tid < tpp * (TILE / (2 * rl))) {
+      const int p = tid / tpp;
+      const int diag = (tid - p * tpp) * ITEMS_M;
+      const int ps = p * 2 * rl;
+      const int m = min(ITEMS_M, 2 * rl - diag);
       const PlainLoad<KeyT> ld(xk);
-      const SmemArray<KeyT> yka(yk + s);
-      const RegularPairs pairs{rl, TILE};
-      merge_thread<ITEMS_M, KeyT>(s, ld, cmp, pairs,
-                                  [&](int i, KeyT k, uint32_t, bool, const PairRange&) { yka.put(i, k); });
+      const SmemArray<KeyT> yka(yk + ps + diag);
+      merge_window<ITEMS_M, KeyT>(ld, cmp, ld.addr(ps), rl, ld.addr(ps + rl), rl, diag, m,
+                                  [&](int i, KeyT k, uint32_t, bool) { yka.put(i, k); });
     }
     __syncthreads();
     cur ^= 1;
