@@ -1,4 +1,8 @@
 // C ABI: 32-bit keys (int32, uint32, float32), keys only.
+#include <algorithm>
+#include <mutex>
+#include <vector>
+
 #include "gms_capi.cuh"
 
 using namespace gms_capi;
@@ -15,7 +19,168 @@ int sort32(void* in, void* out, int64_t n, void* st, int dtype) {
   return run_sort<Eng, uint32_t, NoVal>((uint32_t*)in, nullptr, (uint32_t*)out, nullptr, n, (cudaStream_t)st, dtype);
 }
 
+// ---- host-to-host sorts: copy in, sort, copy out, pipelined ----
+//
+// Per (device, stream): an input-copy stream and an output-copy stream, and
+// two slots of device buffers (input/scratch and output) used alternately, so
+// that the input copy of call i+1 and the output copy of call i-1 overlap the
+// sort of call i.  Within one call the input arrives in kChunks pieces and the
+// base case sorts each piece's tiles as soon as it lands.
+constexpr int kChunks = 8;
+
+struct HostPipe {
+  int dev = 0;
+  cudaStream_t st = nullptr;
+  cudaStream_t h2d = nullptr, d2h = nullptr;
+  void* din[2] = {nullptr, nullptr};
+  void* dout[2] = {nullptr, nullptr};
+  size_t cap = 0;
+  cudaEvent_t ready[2][kChunks];
+  cudaEvent_t sorted[2];
+  cudaEvent_t drained[2];
+  bool used[2] = {false, false};
+  uint64_t calls = 0;
+};
+
+std::mutex g_pipe_mu;
+std::vector<HostPipe*> g_pipes;
+
+int pipe_for(cudaStream_t st, HostPipe** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_error(e, "cudaGetDevice");
+  for (HostPipe* p : g_pipes) {
+    if (p->dev == dev && p->st == st) {
+      *out = p;
+      return GMS_OK;
+    }
+  }
+  HostPipe* p = new HostPipe();
+  p->dev = dev;
+  p->st = st;
+  e = cudaStreamCreateWithFlags(&p->h2d, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->d2h, cudaStreamNonBlocking);
+  for (int s = 0; s < 2 && e == cudaSuccess; ++s) {
+    for (int c = 0; c < kChunks && e == cudaSuccess; ++c) e = cudaEventCreateWithFlags(&p->ready[s][c], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->sorted[s], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->drained[s], cudaEventDisableTiming);
+  }
+  if (e != cudaSuccess) {
+    delete p;  // the few handles created before the failure stay allocated
+    return cuda_error(e, "host pipeline setup");
+  }
+  g_pipes.push_back(p);
+  *out = p;
+  return GMS_OK;
+}
+
+int host_sort_enqueue(const int32_t* host_in, int32_t* host_out, int64_t n, cudaStream_t st) {
+  clear_error();
+  if (n < 0) return set_error(GMS_ERR_INVALID, "n < 0");
+  if (n == 0) return GMS_OK;
+  if (!host_in || !host_out) return set_error(GMS_ERR_INVALID, "null pointer");
+  std::lock_guard<std::mutex> g(g_pipe_mu);
+  HostPipe* p = nullptr;
+  int status = pipe_for(st, &p);
+  if (status != GMS_OK) return status;
+  const size_t bytes = sizeof(int32_t) * (size_t)n;
+  cudaError_t e = cudaSuccess;
+  if (bytes > p->cap) {
+    // growing: wait for every call in flight on this pipeline, then reallocate
+    e = cudaStreamSynchronize(p->h2d);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(p->d2h);
+    if (e != cudaSuccess) return cuda_error(e, "host pipeline drain");
+    for (int s = 0; s < 2; ++s) {
+      cudaFree(p->din[s]);
+      cudaFree(p->dout[s]);
+      p->din[s] = p->dout[s] = nullptr;
+    }
+    p->cap = 0;
+    for (int s = 0; s < 2 && e == cudaSuccess; ++s) {
+      e = cudaMalloc(&p->din[s], bytes);
+      if (e == cudaSuccess) e = cudaMalloc(&p->dout[s], bytes);
+    }
+    if (e != cudaSuccess) return cuda_error(e, "host pipeline buffers");
+    p->cap = bytes;
+  }
+  const int slot = (int)(p->calls++ & 1);
+  // the slot's previous call must have drained its output before reuse
+  if (p->used[slot]) {
+    e = cudaStreamWaitEvent(p->h2d, p->drained[slot], 0);
+    if (e != cudaSuccess) return cuda_error(e, "cudaStreamWaitEvent");
+  }
+  const int64_t tiles = gms::ceil_div(n, EngI32::BASE_TILE);
+  gms::BaseGate gate;
+  gate.chunks = (int)std::min<int64_t>(kChunks, tiles);
+  gate.tiles_per_chunk = gms::ceil_div(tiles, (int64_t)gate.chunks);
+  gate.ready = p->ready[slot];
+  for (int c = 0; c < gate.chunks; ++c) {
+    const int64_t k0 = std::min(n, c * gate.tiles_per_chunk * EngI32::BASE_TILE);
+    const int64_t k1 = std::min(n, (c + 1) * gate.tiles_per_chunk * EngI32::BASE_TILE);
+    if (k1 > k0) {
+      e = cudaMemcpyAsync((int32_t*)p->din[slot] + k0, host_in + k0, sizeof(int32_t) * (size_t)(k1 - k0),
+                          cudaMemcpyHostToDevice, p->h2d);
+      if (e != cudaSuccess) return cuda_error(e, "cudaMemcpyAsync H2D");
+    }
+    e = cudaEventRecord(p->ready[slot][c], p->h2d);
+    if (e != cudaSuccess) return cuda_error(e, "cudaEventRecord");
+  }
+  status = run_sort<EngI32, uint32_t, NoVal>((uint32_t*)p->din[slot], nullptr, (uint32_t*)p->dout[slot], nullptr, n, st,
+                                             0, nullptr, 0, &gate);
+  if (status != GMS_OK) return status;
+  e = cudaEventRecord(p->sorted[slot], st);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(p->d2h, p->sorted[slot], 0);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(host_out, p->dout[slot], bytes, cudaMemcpyDeviceToHost, p->d2h);
+  if (e == cudaSuccess) e = cudaEventRecord(p->drained[slot], p->d2h);
+  if (e != cudaSuccess) return cuda_error(e, "host pipeline output");
+  p->used[slot] = true;
+  return GMS_OK;
+}
+
+int host_sync(cudaStream_t st) {
+  clear_error();
+  std::lock_guard<std::mutex> g(g_pipe_mu);
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_error(e, "cudaGetDevice");
+  for (HostPipe* p : g_pipes) {
+    if (p->dev == dev && p->st == st) {
+      e = cudaStreamSynchronize(p->h2d);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(p->d2h);
+      if (e != cudaSuccess) return cuda_error(e, "host pipeline sync");
+      return GMS_OK;
+    }
+  }
+  e = cudaStreamSynchronize(st);
+  return e == cudaSuccess ? GMS_OK : cuda_error(e, "cudaStreamSynchronize");
+}
+
 }  // namespace
+
+void gms_capi::release_host_pipes() {
+  std::lock_guard<std::mutex> g(g_pipe_mu);
+  for (HostPipe* p : g_pipes) {
+    int cur = 0;
+    cudaGetDevice(&cur);
+    cudaSetDevice(p->dev);
+    cudaStreamSynchronize(p->h2d);
+    cudaStreamSynchronize(p->d2h);
+    for (int s = 0; s < 2; ++s) {
+      cudaFree(p->din[s]);
+      cudaFree(p->dout[s]);
+      for (int c = 0; c < kChunks; ++c) cudaEventDestroy(p->ready[s][c]);
+      cudaEventDestroy(p->sorted[s]);
+      cudaEventDestroy(p->drained[s]);
+    }
+    cudaStreamDestroy(p->h2d);
+    cudaStreamDestroy(p->d2h);
+    cudaSetDevice(cur);
+    delete p;
+  }
+  g_pipes.clear();
+}
 
 int gms_capi::sort32_ws(int dtype, void* in, void* out, int64_t n, void* ws, size_t bytes, cudaStream_t st) {
   uint32_t* i = (uint32_t*)in;
@@ -107,26 +272,16 @@ int gms_find_partitions_i32(const int32_t* task, int64_t size, int k, int64_t ta
   return e == cudaSuccess ? GMS_OK : cuda_error(e, "corank_kernel");
 }
 
+int gms_sort_host_i32_async(const int32_t* host_in, int32_t* host_out, int64_t n, void* stv) {
+  return host_sort_enqueue(host_in, host_out, n, (cudaStream_t)stv);
+}
+
+int gms_host_sync(void* stv) { return host_sync((cudaStream_t)stv); }
+
 int gms_sort_host_i32(const int32_t* host_in, int32_t* host_out, int64_t n, void* stv) {
-  clear_error();
-  if (n < 0) return set_error(GMS_ERR_INVALID, "n < 0");
-  if (n == 0) return GMS_OK;
-  if (!host_in || !host_out) return set_error(GMS_ERR_INVALID, "null pointer");
-  cudaStream_t st = (cudaStream_t)stv;
-  int status = GMS_OK;
-  const size_t bytes = sizeof(int32_t) * (size_t)n;
-  void* din = cache_get(10, bytes, st, &status);
+  const int status = host_sort_enqueue(host_in, host_out, n, (cudaStream_t)stv);
   if (status != GMS_OK) return status;
-  void* dout = cache_get(11, bytes, st, &status);
-  if (status != GMS_OK) return status;
-  cudaError_t e = cudaMemcpyAsync(din, host_in, bytes, cudaMemcpyHostToDevice, st);
-  if (e != cudaSuccess) return cuda_error(e, "cudaMemcpyAsync H2D");
-  status = sort32<EngI32>(din, dout, n, st, 0);
-  if (status != GMS_OK) return status;
-  e = cudaMemcpyAsync(host_out, dout, bytes, cudaMemcpyDeviceToHost, st);
-  if (e != cudaSuccess) return cuda_error(e, "cudaMemcpyAsync D2H");
-  e = cudaStreamSynchronize(st);
-  return e == cudaSuccess ? GMS_OK : cuda_error(e, "cudaStreamSynchronize");
+  return host_sync((cudaStream_t)stv);
 }
 
 }  // extern "C"

@@ -187,6 +187,16 @@ inline cudaError_t ensure_smem(const void* kern, size_t bytes) {
 //   Cmp    strict weak order on K
 //   Codec  user bits <-> K
 //   STABLE stable base case (key/value sorts, user comparators)
+// Host-fed base case: before the base case sorts the tiles of chunk c it makes
+// the stream wait for ready[c] (that chunk's input copy), so copies of later
+// chunks overlap the sorting of earlier ones.  Chunk c covers base tiles
+// [c * tiles_per_chunk, (c + 1) * tiles_per_chunk).
+struct BaseGate {
+  int chunks = 0;
+  int64_t tiles_per_chunk = 0;
+  const cudaEvent_t* ready = nullptr;
+};
+
 template <class KeyT, class V, class Cmp, class Codec, bool STABLE, int NT, int ITEMS, int NTM = NT,
           int ITEMSM = ITEMS>
 struct Engine {
@@ -393,7 +403,7 @@ struct Engine {
   // Full sort.  Result in `out` (keys) / `vout` (payload); `in`/`vin` are
   // clobbered.  enc/dec: apply the codec on the first load / last store.
   static cudaError_t sort(const WsPtrs<KeyT>& w, KeyT* in, V* vin, KeyT* out, V* vout, int64_t n, const Tune& t,
-                          cudaStream_t st) {
+                          cudaStream_t st, const BaseGate* gate = nullptr) {
     if (n <= 0) return cudaSuccess;
     const int P = passes_for(n, t.k);
     KeyT* buf[2] = {in, out};
@@ -417,11 +427,29 @@ struct Engine {
       a.out_run_len = BASE_TILE;
       a.sample_run_len = ceil_div(BASE_TILE, t.sample_b);
       a.sample_out = (P > 0) ? w.s1[0] : nullptr;
-      cudaError_t e;
+      cudaError_t e = cudaSuccess;
       if constexpr (kWarpBase) {
-        e = launch_base_warp(a, ceil_div(n, BASE_TILE), st);
+        const int64_t tiles = ceil_div(n, BASE_TILE);
+        if (!gate) {
+          e = launch_base_warp(a, tiles, st);
+        } else {
+          for (int c = 0; c < gate->chunks && e == cudaSuccess; ++c) {
+            const int64_t t0 = c * gate->tiles_per_chunk;
+            if (t0 >= tiles) break;
+            const int64_t t1 = std::min(tiles, t0 + gate->tiles_per_chunk);
+            e = cudaStreamWaitEvent(st, gate->ready[c], 0);
+            if (e != cudaSuccess) break;
+            TileArgs<KeyT, V> b = a;
+            b.in = a.in + t0 * BASE_TILE;
+            b.out = a.out + t0 * BASE_TILE;
+            b.n = std::min(n, t1 * BASE_TILE) - t0 * BASE_TILE;
+            b.sample_out = a.sample_out ? a.sample_out + t0 * a.sample_run_len : nullptr;
+            e = launch_base_warp(b, t1 - t0, st);
+          }
+        }
       } else {
-        e = launch_tile<MODE_BASE>(a, ceil_div(n, CAP), st);
+        for (int c = 0; gate && c < gate->chunks && e == cudaSuccess; ++c) e = cudaStreamWaitEvent(st, gate->ready[c], 0);
+        if (e == cudaSuccess) e = launch_tile<MODE_BASE>(a, ceil_div(n, CAP), st);
       }
       if (e != cudaSuccess) return e;
     }

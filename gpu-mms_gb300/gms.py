@@ -132,6 +132,8 @@ SIGNATURES = {
     "gms_sort_kv_u64_i32": (_i32, [_vp, _vp, _vp, _vp, _i64, _i32, _vp]),
     "gms_sort_kv_f64_i32": (_i32, [_vp, _vp, _vp, _vp, _i64, _i32, _vp]),
     "gms_sort_host_i32": (_i32, [_vp, _vp, _i64, _vp]),
+    "gms_sort_host_i32_async": (_i32, [_vp, _vp, _i64, _vp]),
+    "gms_host_sync": (_i32, [_vp]),
     "gms_sort_i32_noalloc": (_i32, [_vp, _vp, _i64, _vp]),
     "gms_sort_host_kv_u64_i32": (_i32, [_vp, _vp, _vp, _vp, _i64, _vp]),
     "gms_segmented_sort_i32": (_i32, [_vp, _vp, _i64, _vp, _i64, _vp]),

@@ -113,11 +113,22 @@ int gms_sort_i32_noalloc(int32_t* input, int32_t* output, int64_t n, void* strea
  * sort, copy the result to `host_out` (may equal host_in), and wait for the
  * stream.  Device buffers come from the library's per-stream cache (allocated
  * on first use, reused afterwards).  Pinned host memory gives full copy speed.
+ * gms_sort_host_i32 copies the input in 8 pieces on a second stream and sorts
+ * each piece's base tiles as soon as it lands.
  *
  * Replaces: the reference's driver sequence cudaMemcpy H2D -> multimergesort
  * -> cudaMemcpy D2H, src/testMM.cu:167-195.
  * ------------------------------------------------------------------------- */
 int gms_sort_host_i32(const int32_t* host_in, int32_t* host_out, int64_t n, void* stream);
+/* Pipelined form (no reference counterpart): enqueues the same copy-in, sort
+ * and copy-out and returns at once; `host_out` holds the result, and `host_in`
+ * may be reused, after gms_host_sync(stream).  Two calls can be in flight per
+ * stream: the input copy of one call and the output copy of the one before it
+ * overlap the sort of the other.  The input copy is not ordered after earlier
+ * work on `stream`, so `host_in` must be ready when the call is made.  Use
+ * pinned host memory (pageable memory makes the copies synchronous). */
+int gms_sort_host_i32_async(const int32_t* host_in, int32_t* host_out, int64_t n, void* stream);
+int gms_host_sync(void* stream);
 int gms_sort_host_kv_u64_i32(const uint64_t* keys_in, const int32_t* vals_in, uint64_t* keys_out,
                              int32_t* vals_out, int64_t n, void* stream);
 

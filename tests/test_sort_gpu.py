@@ -319,3 +319,32 @@ def test_sort_with_explicit_workspace(gms, oracle, dtype, kv):
         assert np.array_equal(vout.cpu().numpy(), wv)
     else:
         assert np.array_equal(got.view(np.uint8), oracle.sort(keys).view(np.uint8))
+
+
+# Host-to-host sorts: the synchronous call (input copied in pieces that the base
+# case sorts as they land) and the pipelined call with two sorts in flight.
+def test_host_sort_pipelined(gms, oracle):
+    lib = gms.load()
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    for n in (1, 8191, 8193, 3 * 8192 + 5, 1_000_003):
+        a = oracle.gen_i32(n, 6, n)
+        hin = torch.from_numpy(a).pin_memory()
+        hout = torch.empty_like(hin).pin_memory()
+        assert lib.gms_sort_host_i32(hin.data_ptr(), hout.data_ptr(), n, st) == 0, lib.gms_last_error()
+        assert np.array_equal(hout.numpy(), oracle.sort(a)), n
+    n = 2_500_001
+    ins = [oracle.gen_i32(n, d, 30 + d) for d in range(5)]
+    hins = [torch.from_numpy(x).pin_memory() for x in ins]
+    houts = [torch.empty_like(h).pin_memory() for h in hins]
+    for h, o in zip(hins, houts):
+        assert lib.gms_sort_host_i32_async(h.data_ptr(), o.data_ptr(), n, st) == 0, lib.gms_last_error()
+    assert lib.gms_host_sync(st) == 0
+    for x, o in zip(ins, houts):
+        assert np.array_equal(o.numpy(), oracle.sort(x))
+    # a larger call after smaller ones regrows the pipeline's buffers
+    big = oracle.gen_i32(4_000_000, 0, 99)
+    hb = torch.from_numpy(big).pin_memory()
+    ob = torch.empty_like(hb).pin_memory()
+    assert lib.gms_sort_host_i32_async(hb.data_ptr(), ob.data_ptr(), big.size, st) == 0
+    assert lib.gms_host_sync(st) == 0
+    assert np.array_equal(ob.numpy(), oracle.sort(big))
