@@ -55,7 +55,7 @@ int sort_kv_ws(int dtype, void* ki, int32_t* vi, void* ko, int32_t* vo, int64_t 
 // given, with the caller's scratch (its status word cleared first).
 template <class Eng, class K, class V>
 int run_sort(K* in, V* vin, K* out, V* vout, int64_t n, cudaStream_t st, int dtype, void* user_ws = nullptr,
-             size_t user_bytes = 0, const gms::BaseGate* gate = nullptr) {
+             size_t user_bytes = 0, const gms::BaseGate* gate = nullptr, const gms::RoundSplit* split = nullptr) {
   clear_error();
   if (n < 0) return set_error(GMS_ERR_INVALID, "n < 0");
   if (n == 0) return GMS_OK;
@@ -83,7 +83,7 @@ int run_sort(K* in, V* vin, K* out, V* vout, int64_t n, cudaStream_t st, int dty
     if (status != GMS_OK) return status;
   }
   const gms::WsPtrs<K> w = gms::ws_carve<K>(l, t.k, ws);
-  cudaError_t e = Eng::sort(w, in, vin, out, vout, n, t, st, gate);
+  cudaError_t e = Eng::sort(w, in, vin, out, vout, n, t, st, gate, split);
   if (e != cudaSuccess) return cuda_error(e, "sort");
   return GMS_OK;
 }

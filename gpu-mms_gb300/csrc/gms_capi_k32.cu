@@ -27,6 +27,7 @@ int sort32(void* in, void* out, int64_t n, void* st, int dtype) {
 // sort of call i.  Within one call the input arrives in kChunks pieces and the
 // base case sorts each piece's tiles as soon as it lands.
 constexpr int kChunks = 8;
+constexpr int kOutParts = 8;  // parts of the last merge round
 
 struct HostPipe {
   int dev = 0;
@@ -36,6 +37,7 @@ struct HostPipe {
   void* dout[2] = {nullptr, nullptr};
   size_t cap = 0;
   cudaEvent_t ready[2][kChunks];
+  cudaEvent_t part[2][kOutParts];
   cudaEvent_t sorted[2];
   cudaEvent_t drained[2];
   bool used[2] = {false, false};
@@ -44,6 +46,31 @@ struct HostPipe {
 
 std::mutex g_pipe_mu;
 std::vector<HostPipe*> g_pipes;
+
+// Copies out the final prefix of the output after each part of the last
+// round: records an event on the sort stream, and the output-copy stream
+// waits for it before copying [done, safe).
+struct OutDrain {
+  HostPipe* p;
+  int slot;
+  int32_t* host_out;
+  const int32_t* dev_out;
+  int64_t done;
+  cudaError_t err;
+  int used = 0;
+  static void after_part(void* ctx, int64_t safe, cudaStream_t st) {
+    OutDrain* d = static_cast<OutDrain*>(ctx);
+    if (d->err != cudaSuccess || safe <= d->done || d->used >= kOutParts) return;
+    cudaEvent_t ev = d->p->part[d->slot][d->used++];
+    cudaError_t e = cudaEventRecord(ev, st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(d->p->d2h, ev, 0);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(d->host_out + d->done, d->dev_out + d->done, sizeof(int32_t) * (size_t)(safe - d->done),
+                          cudaMemcpyDeviceToHost, d->p->d2h);
+    if (e == cudaSuccess) d->done = safe;
+    d->err = e;
+  }
+};
 
 int pipe_for(cudaStream_t st, HostPipe** out) {
   int dev = 0;
@@ -62,6 +89,7 @@ int pipe_for(cudaStream_t st, HostPipe** out) {
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->d2h, cudaStreamNonBlocking);
   for (int s = 0; s < 2 && e == cudaSuccess; ++s) {
     for (int c = 0; c < kChunks && e == cudaSuccess; ++c) e = cudaEventCreateWithFlags(&p->ready[s][c], cudaEventDisableTiming);
+    for (int c = 0; c < kOutParts && e == cudaSuccess; ++c) e = cudaEventCreateWithFlags(&p->part[s][c], cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->sorted[s], cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->drained[s], cudaEventDisableTiming);
   }
@@ -126,12 +154,23 @@ int host_sort_enqueue(const int32_t* host_in, int32_t* host_out, int64_t n, cuda
     e = cudaEventRecord(p->ready[slot][c], p->h2d);
     if (e != cudaSuccess) return cuda_error(e, "cudaEventRecord");
   }
+  // Output copy: the last merge round runs in parts, and after each part the
+  // keys known to be final (a prefix of the output) are copied out while the
+  // next part merges; the rest follows the sort.
+  OutDrain drain{p, slot, host_out, (const int32_t*)p->dout[slot], 0, cudaSuccess};
+  gms::RoundSplit split;
+  split.parts = kOutParts;
+  split.after = &OutDrain::after_part;
+  split.ctx = &drain;
   status = run_sort<EngI32, uint32_t, NoVal>((uint32_t*)p->din[slot], nullptr, (uint32_t*)p->dout[slot], nullptr, n, st,
-                                             0, nullptr, 0, &gate);
+                                             0, nullptr, 0, &gate, &split);
   if (status != GMS_OK) return status;
+  if (drain.err != cudaSuccess) return cuda_error(drain.err, "host pipeline output");
   e = cudaEventRecord(p->sorted[slot], st);
   if (e == cudaSuccess) e = cudaStreamWaitEvent(p->d2h, p->sorted[slot], 0);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(host_out, p->dout[slot], bytes, cudaMemcpyDeviceToHost, p->d2h);
+  if (e == cudaSuccess && drain.done < n)
+    e = cudaMemcpyAsync(host_out + drain.done, (const int32_t*)p->dout[slot] + drain.done,
+                        sizeof(int32_t) * (size_t)(n - drain.done), cudaMemcpyDeviceToHost, p->d2h);
   if (e == cudaSuccess) e = cudaEventRecord(p->drained[slot], p->d2h);
   if (e != cudaSuccess) return cuda_error(e, "host pipeline output");
   p->used[slot] = true;
@@ -171,6 +210,7 @@ void gms_capi::release_host_pipes() {
       cudaFree(p->din[s]);
       cudaFree(p->dout[s]);
       for (int c = 0; c < kChunks; ++c) cudaEventDestroy(p->ready[s][c]);
+      for (int c = 0; c < kOutParts; ++c) cudaEventDestroy(p->part[s][c]);
       cudaEventDestroy(p->sorted[s]);
       cudaEventDestroy(p->drained[s]);
     }

@@ -38,6 +38,7 @@ struct TileArgs {
   const int64_t* doff;
   int64_t tiles_full;  // tiles of a full group
   int64_t tiles_last;  // tiles of the last group
+  int64_t tile_base;   // merge_tiles_kernel: tile index of block 0 (a launch may cover part of a round)
   int64_t groups;
   // block sample of the output runs (for the next round); null if unused
   KeyT* sample_out;
@@ -507,7 +508,7 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
   const int lane = tid & 31;
   const int nk = a.k;
 
-  const int64_t tau = blockIdx.x;
+  const int64_t tau = a.tile_base + blockIdx.x;
   if (tau >= total_tiles) return;
   const int64_t g = tau / a.tiles_full;
   const int64_t j = tau - g * a.tiles_full;

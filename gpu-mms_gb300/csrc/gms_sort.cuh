@@ -197,6 +197,19 @@ struct BaseGate {
   const cudaEvent_t* ready = nullptr;
 };
 
+// Last round in parts: the tile merge of a single-group round is launched in
+// `parts` pieces of consecutive tiles, and after each piece `after(ctx, safe,
+// stream)` is called with a count of leading output keys that are final once
+// the piece has run.  Tiles of one group write consecutive output ranges in
+// tile order, and tile T starts at or after (T*G - K)*B keys (each run has at
+// most one partial sample block ahead of boundary T), so after tiles [0, T)
+// at least that prefix is final.
+struct RoundSplit {
+  int parts = 0;
+  void (*after)(void* ctx, int64_t safe, cudaStream_t st) = nullptr;
+  void* ctx = nullptr;
+};
+
 template <class KeyT, class V, class Cmp, class Codec, bool STABLE, int NT, int ITEMS, int NTM = NT,
           int ITEMSM = ITEMS>
 struct Engine {
@@ -309,17 +322,20 @@ struct Engine {
 
   // Bulk-copy merge of the forecast tiles of one round (one CTA per tile).
   template <class VV>
+  // Launches blocks for tiles [a.tile_base, a.tile_base + grid) of a round
+  // with `total_tiles` tiles (grid defaults to all of them).
   static cudaError_t launch_merge_tiles(const TileArgs<KeyT, VV>& a, int64_t total_tiles, cudaStream_t st,
-                                        int level) {
-    if (total_tiles <= 0) return cudaSuccess;
-    if (total_tiles > 0x7fffffff) return cudaErrorInvalidConfiguration;
+                                        int level, int64_t grid = -1) {
+    if (grid < 0) grid = total_tiles - a.tile_base;
+    if (grid <= 0) return cudaSuccess;
+    if (grid > 0x7fffffff) return cudaErrorInvalidConfiguration;
     auto kern = merge_tiles_kernel<KeyT, VV, Cmp, Codec, NTM, ITEMSM>;
     const size_t smem = MergeSmemLayout<KeyT, VV, CAPM>::bytes;
     cudaError_t e = ensure_smem((const void*)kern, smem);
     if (e != cudaSuccess) return e;
     const int kc = level == 0 ? KC_MERGE : KC_SAMPLE_MERGE;
     hook_before(kc, st);
-    kern<<<(unsigned)total_tiles, NTM, smem, st>>>(a, total_tiles);
+    kern<<<(unsigned)grid, NTM, smem, st>>>(a, total_tiles);
     e = cudaGetLastError();
     hook_after(kc, st);
     return e;
@@ -331,7 +347,7 @@ struct Engine {
   template <class VV>
   static cudaError_t round(const WsPtrs<KeyT>& w, int level, const KeyT* in, const VV* vin, KeyT* out, VV* vout, int64_t n,
                            int64_t L, const Tune& t, const KeyT* sample_in, KeyT* sample_out, int enc, int dec,
-                           int gen_index, cudaStream_t st) {
+                           int gen_index, cudaStream_t st, const RoundSplit* split = nullptr) {
     const int k = t.k;
     const int sb = t.sample_b;
     TileArgs<KeyT, VV> a{};
@@ -396,26 +412,52 @@ struct Engine {
     a.tiles_full = tiles_full;
     a.tiles_last = tiles_last;
     a.groups = groups;
+    if (t.bulk_copy && split && split->parts > 1 && groups == 1 && tiles_last > 1) {
+      const int64_t per = ceil_div(tiles_last, (int64_t)split->parts);
+      for (int64_t t0 = 0; t0 < tiles_last; t0 += per) {
+        const int64_t t1 = std::min(tiles_last, t0 + per);
+        TileArgs<KeyT, VV> b = a;
+        b.tile_base = t0;
+        e = launch_merge_tiles(b, t1, st, level, t1 - t0);
+        if (e != cudaSuccess) return e;
+        const int64_t safe = (t1 == tiles_last) ? n : std::max<int64_t>(0, (t1 * G - k) * (int64_t)sb);
+        split->after(split->ctx, std::min(safe, n), st);
+      }
+      return cudaSuccess;
+    }
     if (t.bulk_copy) return launch_merge_tiles(a, groups * tiles_full, st, level);
     return launch_tile<MODE_TILE>(a, groups * tiles_full, st, level);
   }
 
   // Full sort.  Result in `out` (keys) / `vout` (payload); `in`/`vin` are
-  // clobbered.  enc/dec: apply the codec on the first load / last store.
+  // clobbered.  The base case runs in place when the round count is odd, so
+  // the last round lands in `out`.
   static cudaError_t sort(const WsPtrs<KeyT>& w, KeyT* in, V* vin, KeyT* out, V* vout, int64_t n, const Tune& t,
-                          cudaStream_t st, const BaseGate* gate = nullptr) {
+                          cudaStream_t st, const BaseGate* gate = nullptr, const RoundSplit* split = nullptr) {
+    const bool odd = passes_for(n, t.k) % 2 == 1;
+    return sort_to(w, in, vin, odd ? in : out, odd ? vin : vout, odd ? out : in, odd ? vout : vin, out, vout, n, t, st,
+                   gate, split);
+  }
+
+  // Full sort with explicit buffers: the base case reads `src` and writes
+  // `d0` (or `dst` when no merge round follows), rounds ping-pong between `d0`
+  // and `d1`, and the last round writes `dst`.  `src` may equal `d0`; `dst`
+  // must differ from the last round's input (d0 when the round count is odd,
+  // d1 when it is even) and may be any memory the kernels can store to,
+  // mapped pinned host memory included.
+  static cudaError_t sort_to(const WsPtrs<KeyT>& w, const KeyT* src, const V* vsrc, KeyT* d0, V* vd0, KeyT* d1, V* vd1,
+                             KeyT* dst, V* vdst, int64_t n, const Tune& t, cudaStream_t st,
+                             const BaseGate* gate = nullptr, const RoundSplit* split = nullptr) {
     if (n <= 0) return cudaSuccess;
     const int P = passes_for(n, t.k);
-    KeyT* buf[2] = {in, out};
-    V* vbuf[2] = {vin, vout};
-    // base case: P odd -> in place on `in`; P even -> `in` to `out`
-    int cur = (P % 2 == 1) ? 0 : 1;
+    KeyT* buf[2] = {d0, d1};
+    V* vbuf[2] = {vd0, vd1};
     {
       TileArgs<KeyT, V> a{};
-      a.in = in;
-      a.out = buf[cur];
-      a.vin = vin;
-      a.vout = vbuf[cur];
+      a.in = src;
+      a.out = P > 0 ? d0 : dst;
+      a.vin = vsrc;
+      a.vout = P > 0 ? vd0 : vdst;
       a.n = n;
       a.L = BASE_TILE;
       a.k = 1;
@@ -453,13 +495,16 @@ struct Engine {
       }
       if (e != cudaSuccess) return e;
     }
+    int cur = 0;
     int sbuf = 0;
     int64_t L = BASE_TILE;
     for (int p = 0; p < P; ++p) {
       const bool last = (p == P - 1);
       KeyT* sout = last ? nullptr : w.s1[sbuf ^ 1];
-      cudaError_t e = round<V>(w, 0, buf[cur], vbuf[cur], buf[cur ^ 1], vbuf[cur ^ 1], n, L, t, w.s1[sbuf], sout, 0,
-                               last ? 1 : 0, 0, st);
+      KeyT* o = last ? dst : buf[cur ^ 1];
+      V* vo = last ? vdst : vbuf[cur ^ 1];
+      cudaError_t e = round<V>(w, 0, buf[cur], vbuf[cur], o, vo, n, L, t, w.s1[sbuf], sout, 0, last ? 1 : 0, 0, st,
+                               last ? split : nullptr);
       if (e != cudaSuccess) return e;
       cur ^= 1;
       sbuf ^= 1;

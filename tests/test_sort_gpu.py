@@ -332,6 +332,12 @@ def test_host_sort_pipelined(gms, oracle):
         hout = torch.empty_like(hin).pin_memory()
         assert lib.gms_sort_host_i32(hin.data_ptr(), hout.data_ptr(), n, st) == 0, lib.gms_last_error()
         assert np.array_equal(hout.numpy(), oracle.sort(a)), n
+        pageable = np.empty(n, dtype=np.int32)  # pageable output memory
+        assert lib.gms_sort_host_i32(hin.data_ptr(), pageable.ctypes.data, n, st) == 0, lib.gms_last_error()
+        assert np.array_equal(pageable, oracle.sort(a)), n
+        inplace = torch.from_numpy(a.copy()).pin_memory()  # output over the input
+        assert lib.gms_sort_host_i32(inplace.data_ptr(), inplace.data_ptr(), n, st) == 0
+        assert np.array_equal(inplace.numpy(), oracle.sort(a)), n
     n = 2_500_001
     ins = [oracle.gen_i32(n, d, 30 + d) for d in range(5)]
     hins = [torch.from_numpy(x).pin_memory() for x in ins]
