@@ -6,22 +6,37 @@
 #include <cstdint>
 #include <cstdio>
 #include <string>
+#include <type_traits>
 
 #include "../../include/gms.h"
 #include "gms_sort.cuh"
 
 namespace gms_capi {
 
-// Engines of the prebuilt dtypes.  32-bit keys and 64-bit keys share one
-// geometry: 512 threads x 17 keys = 8704-key tiles (17 is odd, so the
-// thread-strided shared-memory accesses of a warp fall in distinct banks).
+// Engines of the prebuilt dtypes.  Item counts per thread are odd, so the
+// thread-strided shared-memory accesses of a warp fall in distinct banks.
+// Geometries were chosen by timing on GB300 (2^28 int32 keys, 2^27 uint64
+// keys, 2^27 uint64 / float32 keys with int32 payload):
+//   keys only   base: warp-shuffle base case (8192-key tiles); 512 x 17 for
+//               tile_sort; data rounds 288 x 29 (32-bit keys: three CTAs of
+//               ~67 KB shared memory per SM) or 256 x 17 (64-bit keys)
+//   key/value   base and data rounds 256 x 17 (keys + payload staged: three
+//               CTAs per SM for 32-bit keys)
+//   index rounds (a block sample merged with its uint32 positions) 256 x 17
 constexpr int kNT = 512;
 constexpr int kItems = 17;
+using IndexGeo = gms::MergeGeo<256, 17>;
+template <class K>
+using KeysGeo = std::conditional_t<sizeof(K) == 4, gms::MergeGeo<288, 29>, gms::MergeGeo<256, 17>>;
 
 template <class K, class Codec>
-using KeysEngine = gms::Engine<K, gms::NoVal, gms::KeyLess, Codec, false, kNT, kItems>;
+using KeysEngine = gms::Engine<K, gms::NoVal, gms::KeyLess, Codec, false, kNT, kItems, KeysGeo<K>, IndexGeo>;
 template <class K, class Codec>
-using KvEngine = gms::Engine<K, int32_t, gms::KeyLess, Codec, true, kNT, kItems>;
+using KvEngine = gms::Engine<K, int32_t, gms::KeyLess, Codec, true, 256, 17, gms::MergeGeo<256, 17>, IndexGeo>;
+
+// Smallest forecast-tile capacity of any prebuilt engine: a tuning must leave
+// room for a tile in every one (capacity / sample_b > k).
+constexpr int kMinTileCap = IndexGeo::CAPW;
 
 // error recording (defined in gms_capi_misc.cu)
 int set_error(int status, const char* msg);

@@ -292,7 +292,7 @@ int gms_find_partitions_i32(const int32_t* task, int64_t size, int k, int64_t ta
   uint32_t* mi = (uint32_t*)(tmp + mk_bytes);
   cudaError_t e = cudaSuccess;
   if (task_size > 0) {
-    const gms::WsLayout l = EngI32::plan_merge_level(task_size, size, t);
+    const gms::WsLayout l = EngI32::plan_merge_level<uint32_t>(task_size, size, t);
     if (!l.ok) return set_error(GMS_ERR_INVALID, "tuning too fine for this task (sample recursion too deep)");
     void* ws = cache_get(0, gms::ws_bytes_for<uint32_t>(l, t.k), st, &status);
     if (status != GMS_OK) return status;

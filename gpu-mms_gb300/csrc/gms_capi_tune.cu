@@ -50,7 +50,7 @@ int size_class(int64_t n) {
 }
 
 bool valid_tune(int k, int sample_b) {
-  return k >= 2 && k <= 32 && sample_b >= 8 && (int64_t)gms::WindowCap<kNT, kItems>::value / sample_b - k >= 1;
+  return k >= 2 && k <= 32 && sample_b >= 8 && (int64_t)kMinTileCap / sample_b - k >= 1;
 }
 
 void table_put(int dtype, int kv, int cls, const gms::Tune& t, double ms) {
@@ -255,7 +255,7 @@ int gms_set_tune(int k, int sample_b, int bulk_copy) {
   clear_error();
   if (k < 2 || k > 32) return set_error(GMS_ERR_INVALID, "k must be in [2, 32]");
   if (!valid_tune(k, sample_b))
-    return set_error(GMS_ERR_INVALID, "sample_b must be >= 8 and leave room for a tile (8432/sample_b > k)");
+    return set_error(GMS_ERR_INVALID, "sample_b must be >= 8 and leave room for a tile (4080/sample_b > k)");
   std::lock_guard<std::mutex> g(g_tune_mu);
   g_tune.k = k;
   g_tune.sample_b = sample_b;

@@ -431,37 +431,66 @@ __device__ __forceinline__ void merge_thread(int s, const Ld& ld, Cmp cmp, const
 // Produces outputs [diag, diag + m) of the stable merge of A (byte address a0,
 // na keys) and B (b0, nb keys), where 0 < m <= ITEMS and diag + m <= na + nb:
 // the window never crosses the end of its pair, so every thread of a warp runs
-// the same code.  Two independent streams (H and ITEMS-H outputs) keep two
-// dependency chains in flight; the second stream's merge-path search scans
-// only the H+1 candidates after the first's co-rank.  Outputs at or past m are
-// computed from in-bounds slack and dropped, never emitted.
-template <int ITEMS, class KeyT, class Ld, class Cmp, class Emit>
+// the same code.  NS independent streams of H = ceil(ITEMS/NS) outputs keep NS
+// dependency chains in flight; stream s's merge-path search scans only the H+1
+// candidates after stream s-1's co-rank.  Outputs at or past m are computed
+// from in-bounds slack and dropped, never emitted.
+template <int ITEMS, class KeyT, int NS = 2, class Ld, class Cmp, class Emit>
 __device__ __forceinline__ void merge_window(const Ld& ld, Cmp cmp, uint32_t A0, int na, uint32_t B0, int nb, int diag,
                                              int m, const Emit& emit) {
-  constexpr int H = (ITEMS + 1) / 2;
+  constexpr int H = (ITEMS + NS - 1) / NS;
   constexpr uint32_t S = sizeof(KeyT);
-  const int ia1 = merge_path<KeyT>(ld, A0, na, B0, nb, diag, cmp);
-  const int d2 = diag + H < na + nb ? diag + H : na + nb;
-  const int lo2 = d2 - nb > ia1 ? d2 - nb : ia1;
-  int hi2 = ia1 + H;
-  hi2 = hi2 < na ? hi2 : na;
-  hi2 = hi2 < d2 ? hi2 : d2;
-  const int ia2 = merge_path_in<KeyT>(ld, A0, B0, d2, lo2, hi2, cmp);
-  const uint32_t EA = A0 + (uint32_t)na * S, EB = B0 + (uint32_t)nb * S;
-  MergeCursor<KeyT> c1, c2;
-  c1.init(ld, A0 + (uint32_t)ia1 * S, EA, B0 + (uint32_t)(diag - ia1) * S, EB);
-  c2.init(ld, A0 + (uint32_t)ia2 * S, EA, B0 + (uint32_t)(d2 - ia2) * S, EB);
+  if constexpr (NS == 2) {
+    const int ia1 = merge_path<KeyT>(ld, A0, na, B0, nb, diag, cmp);
+    const int d2 = diag + H < na + nb ? diag + H : na + nb;
+    const int lo2 = d2 - nb > ia1 ? d2 - nb : ia1;
+    int hi2 = ia1 + H;
+    hi2 = hi2 < na ? hi2 : na;
+    hi2 = hi2 < d2 ? hi2 : d2;
+    const int ia2 = merge_path_in<KeyT>(ld, A0, B0, d2, lo2, hi2, cmp);
+    const uint32_t EA = A0 + (uint32_t)na * S, EB = B0 + (uint32_t)nb * S;
+    MergeCursor<KeyT> c1, c2;
+    c1.init(ld, A0 + (uint32_t)ia1 * S, EA, B0 + (uint32_t)(diag - ia1) * S, EB);
+    c2.init(ld, A0 + (uint32_t)ia2 * S, EA, B0 + (uint32_t)(d2 - ia2) * S, EB);
 #pragma unroll
-  for (int i = 0; i < H; ++i) {
-    uint32_t src1;
-    bool ta1;
-    const KeyT o1 = c1.step(ld, cmp, src1, ta1);
-    if (i < m) emit(i, o1, src1, ta1);
-    if (H + i < ITEMS) {
-      uint32_t src2;
-      bool ta2;
-      const KeyT o2 = c2.step(ld, cmp, src2, ta2);
-      if (H + i < m) emit(H + i, o2, src2, ta2);
+    for (int i = 0; i < H; ++i) {
+      uint32_t src1;
+      bool ta1;
+      const KeyT o1 = c1.step(ld, cmp, src1, ta1);
+      if (i < m) emit(i, o1, src1, ta1);
+      if (H + i < ITEMS) {
+        uint32_t src2;
+        bool ta2;
+        const KeyT o2 = c2.step(ld, cmp, src2, ta2);
+        if (H + i < m) emit(H + i, o2, src2, ta2);
+      }
+    }
+  } else {
+    const uint32_t EA = A0 + (uint32_t)na * S, EB = B0 + (uint32_t)nb * S;
+    MergeCursor<KeyT> c[NS];
+    int ia = merge_path<KeyT>(ld, A0, na, B0, nb, diag, cmp);
+    c[0].init(ld, A0 + (uint32_t)ia * S, EA, B0 + (uint32_t)(diag - ia) * S, EB);
+#pragma unroll
+    for (int q = 1; q < NS; ++q) {
+      const int dq = diag + q * H < na + nb ? diag + q * H : na + nb;
+      const int lo = dq - nb > ia ? dq - nb : ia;
+      int hi = ia + H;
+      hi = hi < na ? hi : na;
+      hi = hi < dq ? hi : dq;
+      ia = merge_path_in<KeyT>(ld, A0, B0, dq, lo, hi, cmp);
+      c[q].init(ld, A0 + (uint32_t)ia * S, EA, B0 + (uint32_t)(dq - ia) * S, EB);
+    }
+#pragma unroll
+    for (int i = 0; i < H; ++i) {
+#pragma unroll
+      for (int q = 0; q < NS; ++q) {
+        if (q * H + i < ITEMS) {
+          uint32_t src;
+          bool ta;
+          const KeyT o = c[q].step(ld, cmp, src, ta);
+          if (q * H + i < m) emit(q * H + i, o, src, ta);
+        }
+      }
     }
   }
 }

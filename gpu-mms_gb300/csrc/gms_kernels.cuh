@@ -424,7 +424,7 @@ __global__ void __launch_bounds__(NT) base_warp_kernel(TileArgs<KeyT, NoVal> a) 
       const int m = min(ITEMS_M, 2 * rl - diag);
       const PlainLoad<KeyT> ld(xk);
       const SmemArray<KeyT> yka(yk + ps + diag);
-      merge_window<ITEMS_M, KeyT>(ld, cmp, ld.addr(ps), rl, ld.addr(ps + rl), rl, diag, m,
+      merge_window<ITEMS_M, KeyT, 2>(ld, cmp, ld.addr(ps), rl, ld.addr(ps + rl), rl, diag, m,
                                   [&](int i, KeyT k, uint32_t, bool) { yka.put(i, k); });
     }
     __syncthreads();
@@ -482,7 +482,7 @@ struct WindowCap {
   static constexpr int value = (NT - 16) * ITEMS;
 };
 
-template <class KeyT, class V, class Cmp, class Codec, int NT, int ITEMS>
+template <class KeyT, class V, class Cmp, class Codec, int NT, int ITEMS, int NS>
 __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, int64_t total_tiles) {
   constexpr int CAP = NT * ITEMS;                        // shared-memory buffers
   constexpr int TILE_MAX = WindowCap<NT, ITEMS>::value;  // keys a tile may hold
@@ -709,7 +709,7 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
         const SmemArray<V> yva(v1 + ps + diag);
         const SmemArray<V> sva(reinterpret_cast<const V*>(stage_v));
         const int gen = a.gen_index;
-        merge_window<ITEMS, KeyT>(ld, cmp, A0, na, B0, nb, diag, m, [&](int i, KeyT k, uint32_t src, bool ta) {
+        merge_window<ITEMS, KeyT, NS>(ld, cmp, A0, na, B0, nb, diag, m, [&](int i, KeyT k, uint32_t src, bool ta) {
           yka.put(i, k);
           if constexpr (kHasVal) {
             const int seg = ta ? si : si + 1;
@@ -725,7 +725,7 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
         const PlainLoad<KeyT> ld(xk);
         const SmemArray<KeyT> yka(yk + ps + diag);
         const SmemArray<V> xva(xv), yva(yv + ps + diag);
-        merge_window<ITEMS, KeyT>(ld, cmp, ld.addr(ps), na, ld.addr(pm), nb, diag, m,
+        merge_window<ITEMS, KeyT, NS>(ld, cmp, ld.addr(ps), na, ld.addr(pm), nb, diag, m,
                                   [&](int i, KeyT k, uint32_t src, bool) {
                                     yka.put(i, k);
                                     if constexpr (kHasVal)

@@ -210,14 +210,31 @@ struct RoundSplit {
   void* ctx = nullptr;
 };
 
-template <class KeyT, class V, class Cmp, class Codec, bool STABLE, int NT, int ITEMS, int NTM = NT,
-          int ITEMSM = ITEMS>
-struct Engine {
-  // base-case tile (NT threads x ITEMS keys) and merge tile (NTM x ITEMSM)
+// Geometry of the merge kernels of one payload type: NT threads x ITEMS keys,
+// NS merge streams per thread.  CAP bounds a group merged by one CTA
+// (tile_kernel), CAPW a forecast tile (merge_tiles_kernel, window-aligned).
+template <int NT_, int ITEMS_, int NS_ = 2>
+struct MergeGeo {
+  static constexpr int NT = NT_;
+  static constexpr int ITEMS = ITEMS_;
+  static constexpr int NS = NS_;
   static constexpr int CAP = NT * ITEMS;
-  static constexpr int CAPM = NTM * ITEMSM;
-  // largest forecast tile: the merge kernel's window-aligned capacity
-  static constexpr int CAPW = WindowCap<NTM, ITEMSM>::value;
+  static constexpr int CAPW = WindowCap<NT, ITEMS>::value;
+};
+
+// MG: merge geometry of the data rounds (payload V); IG: of the rounds that
+// carry a uint32 index payload (merging a block sample with its positions).
+template <class KeyT, class V, class Cmp, class Codec, bool STABLE, int NT, int ITEMS, class MG = MergeGeo<NT, ITEMS>,
+          class IG = MG>
+struct Engine {
+  using IdxT = uint32_t;
+  // geometry of a round whose payload is VV
+  template <class VV>
+  using Geo = std::conditional_t<std::is_same<VV, V>::value, MG, IG>;
+  // base-case tile (NT threads x ITEMS keys)
+  static constexpr int CAP = NT * ITEMS;
+  // smallest forecast tile capacity over both geometries (bounds the tuning)
+  static constexpr int CAPW = MG::CAPW < IG::CAPW ? MG::CAPW : IG::CAPW;
   // Keys-only sorts of 4- and 8-byte integer keys use the warp-shuffle base
   // case: 256 x 32 keys (4-byte) or 512 x 16 keys (8-byte), 8192-key tiles.
   static constexpr bool kWarpBase =
@@ -226,7 +243,6 @@ struct Engine {
   static constexpr int kKPL = sizeof(KeyT) == 4 ? 32 : 16;
   static constexpr int kITB = sizeof(KeyT) == 4 ? 33 : 17;
   static constexpr int BASE_TILE = kWarpBase ? kNTB * kKPL : CAP;
-  using IdxT = uint32_t;
 
   // ---------------- geometry ----------------
   static int passes_for(int64_t n, int k) {
@@ -235,16 +251,18 @@ struct Engine {
     return p;
   }
 
-  // Walks the recursion of one merge round and records scratch sizes.
+  // Walks the recursion of one merge round (payload VV) and records scratch
+  // sizes.
+  template <class VV = V>
   static void plan_round(WsLayout& l, int level, int64_t n, int64_t L, const Tune& t, bool gather0 = false) {
     const int k = t.k;
-    if ((int64_t)k * L <= CAPM) return;  // GROUP mode, no scratch
+    if ((int64_t)k * L <= Geo<VV>::CAP) return;  // GROUP mode, no scratch
     if (level + 1 >= kMaxLevels) {
       l.ok = false;  // sample recursion too deep for this tuning
       return;
     }
     const int sb = t.sample_b;
-    const int64_t G = CAPW / sb - k;
+    const int64_t G = Geo<VV>::CAPW / sb - k;
     const int64_t runs = ceil_div(n, L);
     const int64_t Ls = ceil_div(L, sb);
     const int64_t ns = (runs - 1) * Ls + ceil_div(n - (runs - 1) * L, sb);
@@ -259,22 +277,23 @@ struct Engine {
       l.s[level + 1] = std::max(l.s[level + 1], ns);
     }
     l.depth = std::max(l.depth, level + 1);
-    plan_round(l, level + 1, ns, Ls, t);
+    plan_round<IdxT>(l, level + 1, ns, Ls, t);
   }
 
   static WsLayout plan(int64_t n, const Tune& t) {
     WsLayout l;
     int64_t L = BASE_TILE;
     while (L < n) {
-      plan_round(l, 0, n, L, t);
+      plan_round<V>(l, 0, n, L, t);
       L *= t.k;
     }
     return l;
   }
 
+  template <class VV = V>
   static WsLayout plan_merge_level(int64_t n, int64_t L, const Tune& t) {
     WsLayout l;
-    plan_round(l, 0, n, L, t, true);
+    plan_round<VV>(l, 0, n, L, t, true);
     return l;
   }
 
@@ -283,8 +302,8 @@ struct Engine {
   static cudaError_t launch_tile(const TileArgs<KeyT, VV>& a, int64_t grid, cudaStream_t st, int level = 0) {
     if (grid <= 0) return cudaSuccess;
     constexpr bool kStable = (MODE == MODE_BASE) ? STABLE : false;
-    constexpr int kNT = (MODE == MODE_BASE) ? NT : NTM;
-    constexpr int kIT = (MODE == MODE_BASE) ? ITEMS : ITEMSM;
+    constexpr int kNT = (MODE == MODE_BASE) ? NT : Geo<VV>::NT;
+    constexpr int kIT = (MODE == MODE_BASE) ? ITEMS : Geo<VV>::ITEMS;
     auto kern = tile_kernel<KeyT, VV, Cmp, Codec, MODE, kStable, kNT, kIT>;
     const size_t smem = TileSmemLayout<KeyT, VV, kNT * kIT>::bytes;
     cudaError_t e = ensure_smem((const void*)kern, smem);
@@ -329,13 +348,14 @@ struct Engine {
     if (grid < 0) grid = total_tiles - a.tile_base;
     if (grid <= 0) return cudaSuccess;
     if (grid > 0x7fffffff) return cudaErrorInvalidConfiguration;
-    auto kern = merge_tiles_kernel<KeyT, VV, Cmp, Codec, NTM, ITEMSM>;
-    const size_t smem = MergeSmemLayout<KeyT, VV, CAPM>::bytes;
+    using GG = Geo<VV>;
+    auto kern = merge_tiles_kernel<KeyT, VV, Cmp, Codec, GG::NT, GG::ITEMS, GG::NS>;
+    const size_t smem = MergeSmemLayout<KeyT, VV, GG::CAP>::bytes;
     cudaError_t e = ensure_smem((const void*)kern, smem);
     if (e != cudaSuccess) return e;
     const int kc = level == 0 ? KC_MERGE : KC_SAMPLE_MERGE;
     hook_before(kc, st);
-    kern<<<(unsigned)grid, NTM, smem, st>>>(a, total_tiles);
+    kern<<<(unsigned)grid, GG::NT, smem, st>>>(a, total_tiles);
     e = cudaGetLastError();
     hook_after(kc, st);
     return e;
@@ -367,11 +387,11 @@ struct Engine {
     a.out_run_len = L * k;
     a.sample_run_len = ceil_div(L * k, sb);
     const int64_t groups = ceil_div(n, L * k);
-    if ((int64_t)k * L <= CAPM) {
+    if ((int64_t)k * L <= Geo<VV>::CAP) {
       return launch_tile<MODE_GROUP>(a, groups, st, level);
     }
     if (level + 1 >= kMaxLevels) return cudaErrorInvalidValue;
-    const int64_t G = CAPW / sb - k;
+    const int64_t G = Geo<VV>::CAPW / sb - k;
     const int64_t runs = ceil_div(n, L);
     const int64_t Ls = ceil_div(L, sb);
     const int64_t ns = (runs - 1) * Ls + ceil_div(n - (runs - 1) * L, sb);

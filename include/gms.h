@@ -297,8 +297,8 @@ int gms_timing_reset(void);
  * (scripts/findK.sh, scripts/blocksThreads.sh).
  *   k          fan-in of a merge round, 2..32 (default 32)
  *   sample_b   block size of the forecast sample that cuts tiles (default 32;
- *              8 <= sample_b and 8432/sample_b > k, 8432 keys being the
- *              largest merge tile).  A sort whose sample
+ *              8 <= sample_b and 4080/sample_b > k, 4080 keys being the
+ *              smallest merge-tile capacity of the prebuilt engines).  A sort whose sample
  *              recursion would get too deep for the tuning returns
  *              GMS_ERR_INVALID.
  *   bulk_copy  1: merge kernel staging each tile's segments in shared memory

@@ -22,13 +22,16 @@ class Geometry:
     is checked to need at most nt windows at every merge level; without them
     tiles are cut for cap."""
 
-    def __init__(self, cap, k, b, base=None, nt=None, items=None):
+    def __init__(self, cap, k, b, base=None, nt=None, items=None, sample=None):
         self.cap, self.k, self.b = cap, k, b
         self.base = base or cap
         self.nt, self.items = nt, items
         self.tile_cap = (nt - 16) * items if nt else cap
         self.g = self.tile_cap // b - k
         assert self.g > 0, "tile geometry needs TILE_CAP/B > K"
+        # geometry of the rounds that merge a block sample with its positions
+        # (Engine's index geometry); defaults to this one
+        self.sample = sample or self
 
 
 def windows_per_level(seg_lens, items):
@@ -81,7 +84,7 @@ def model_round(keys, idx, L, geo, stats, level=0):
         S[r * Ls:r * Ls + len(samp)] = samp
         if r < runs - 1:
             assert len(samp) == Ls
-    fk, fi = model_round(S, np.arange(ns, dtype=np.int64), Ls, geo, stats, level + 1)
+    fk, fi = model_round(S, np.arange(ns, dtype=np.int64), Ls, geo.sample, stats, level + 1)
     groups = ceil_div(n, L * k)
     tiles_full = ceil_div(k * Ls, G)
     last_ns = ns - (groups - 1) * k * Ls

@@ -244,7 +244,7 @@ def test_invalid_arguments(gms):
 # ---------------------------------------------------------------------------
 # Tuning: other fan-ins, sample block sizes and both merge paths (bulk-copy
 # staging and plain loads) must give the same bits.
-TUNES = [(32, 32, 0), (2, 32, 1), (3, 16, 1), (7, 64, 1), (16, 8, 1), (32, 128, 1), (5, 100, 0), (32, 17, 1)]
+TUNES = [(32, 32, 0), (2, 32, 1), (3, 16, 1), (7, 64, 1), (16, 8, 1), (32, 96, 1), (5, 100, 0), (32, 17, 1)]
 
 
 @pytest.fixture
@@ -275,7 +275,8 @@ def test_tune_rejects_bad_values(gms, tuned):
     assert lib.gms_set_tune(1, 32, 1) == 1
     assert lib.gms_set_tune(33, 32, 1) == 1
     assert lib.gms_set_tune(32, 0, 1) == 1
-    assert lib.gms_set_tune(32, 300, 1) == 1  # 8704/300 - 32 < 1
+    assert lib.gms_set_tune(32, 300, 1) == 1  # 4080/300 - 32 < 1
+    assert lib.gms_set_tune(32, 128, 1) == 1  # 4080/128 - 32 < 1
 
 
 # Explicit workspace: same bits as the cached-scratch sort, for keys-only and
