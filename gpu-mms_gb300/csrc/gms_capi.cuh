@@ -17,9 +17,10 @@ namespace gms_capi {
 // thread-strided shared-memory accesses of a warp fall in distinct banks.
 // Geometries were chosen by timing on GB300 (2^28 int32 keys, 2^27 uint64
 // keys, 2^27 uint64 / float32 keys with int32 payload):
-//   keys only   base: warp-shuffle base case (8192-key tiles); 512 x 17 for
-//               tile_sort; data rounds 288 x 29 (32-bit keys: three CTAs of
-//               ~67 KB shared memory per SM) or 256 x 17 (64-bit keys)
+//   keys only   base: warp-shuffle base case (8192-key tiles for 32-bit
+//               keys, 4096 for 64-bit keys); 512 x 17 for tile_sort; data
+//               rounds 288 x 29 (32-bit keys: three CTAs of ~67 KB shared
+//               memory per SM) or 256 x 17 (64-bit keys)
 //   key/value   base and data rounds 256 x 17 (keys + payload staged: three
 //               CTAs per SM for 32-bit keys)
 //   index rounds (a block sample merged with its uint32 positions) 256 x 17

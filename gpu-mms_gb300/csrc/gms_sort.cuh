@@ -222,10 +222,24 @@ struct MergeGeo {
   static constexpr int CAPW = WindowCap<NT, ITEMS>::value;
 };
 
+// Geometry of the warp-shuffle base case: NT threads x KPL keys per lane
+// (tile NT*KPL), shared-memory merge levels with ITEMS outputs per thread.
+template <int NT_, int KPL_, int ITEMS_>
+struct WarpBaseGeo {
+  static constexpr int NT = NT_;
+  static constexpr int KPL = KPL_;
+  static constexpr int ITEMS = ITEMS_;
+};
+// 32-bit keys: 8192-key tiles; 64-bit keys: 4096-key tiles (256 threads keep
+// three CTAs per SM within the register file and shared memory).
+template <class KeyT>
+using DefaultWarpBase = std::conditional_t<sizeof(KeyT) == 4, WarpBaseGeo<256, 32, 33>, WarpBaseGeo<256, 16, 33>>;
+
 // MG: merge geometry of the data rounds (payload V); IG: of the rounds that
-// carry a uint32 index payload (merging a block sample with its positions).
+// carry a uint32 index payload (merging a block sample with its positions);
+// WB: warp-shuffle base case (keys-only 4/8-byte integer keys).
 template <class KeyT, class V, class Cmp, class Codec, bool STABLE, int NT, int ITEMS, class MG = MergeGeo<NT, ITEMS>,
-          class IG = MG>
+          class IG = MG, class WB = DefaultWarpBase<KeyT>>
 struct Engine {
   using IdxT = uint32_t;
   // geometry of a round whose payload is VV
@@ -236,12 +250,12 @@ struct Engine {
   // smallest forecast tile capacity over both geometries (bounds the tuning)
   static constexpr int CAPW = MG::CAPW < IG::CAPW ? MG::CAPW : IG::CAPW;
   // Keys-only sorts of 4- and 8-byte integer keys use the warp-shuffle base
-  // case: 256 x 32 keys (4-byte) or 512 x 16 keys (8-byte), 8192-key tiles.
+  // case (geometry WB).
   static constexpr bool kWarpBase =
       !STABLE && !HasVal<V>::value && std::is_integral<KeyT>::value && (sizeof(KeyT) == 4 || sizeof(KeyT) == 8);
-  static constexpr int kNTB = sizeof(KeyT) == 4 ? 256 : 512;
-  static constexpr int kKPL = sizeof(KeyT) == 4 ? 32 : 16;
-  static constexpr int kITB = sizeof(KeyT) == 4 ? 33 : 17;
+  static constexpr int kNTB = WB::NT;
+  static constexpr int kKPL = WB::KPL;
+  static constexpr int kITB = WB::ITEMS;
   static constexpr int BASE_TILE = kWarpBase ? kNTB * kKPL : CAP;
 
   // ---------------- geometry ----------------

@@ -42,6 +42,7 @@ def test_queries_without_gpu(lib):
     assert lib.gms_max_tile() == 512 * 17
     assert lib.gms_rounds(0, 0, 1 << 28) == 3
     assert lib.gms_base_tile(0, 0) == 8192  # keys-only: warp-shuffle base case
+    assert lib.gms_base_tile(4, 0) == 4096  # 64-bit keys: 256 threads x 16 keys
     assert lib.gms_base_tile(0, 1) == 4352  # key/value: stable base case, 256 x 17
     assert lib.gms_rounds(0, 0, 8192) == 0
     assert lib.gms_rounds(0, 0, 8193) == 1
