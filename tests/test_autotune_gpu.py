@@ -77,7 +77,8 @@ def test_autotune_kv_f32(gms, oracle, clean):
 
 
 def test_small_sizes_time_defaults_only(gms, clean):
-    got = gms.autotune("uint64", 5000)  # one base tile, no merge round
+    n = clean.gms_base_tile(4, 0) - 7  # one base tile, no merge round
+    got = gms.autotune("uint64", n)
     assert {k: got[k] for k in DEFAULT} == DEFAULT
 
 
