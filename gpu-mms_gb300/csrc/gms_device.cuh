@@ -354,6 +354,24 @@ struct MergeCursor {
     return o;
   }
 
+  // step() for a cursor that cannot run out of either run before it stops:
+  // no end checks.
+  template <class Ld, class Cmp>
+  __device__ __forceinline__ KeyT step_inner(const Ld& ld, Cmp cmp, uint32_t& src, bool& took_a) {
+    constexpr uint32_t S = sizeof(KeyT);
+    const bool ta = !cmp(kb, ka);
+    const KeyT o = ta ? ka : kb;
+    const uint32_t cur = ta ? xa : xb;
+    const KeyT nv = ld.at(cur + S);
+    xa = ta ? cur + S : xa;
+    xb = ta ? xb : cur + S;
+    ka = ta ? nv : ka;
+    kb = ta ? kb : nv;
+    src = cur;
+    took_a = ta;
+    return o;
+  }
+
   __device__ __forceinline__ bool exhausted() const { return xa + xb == ea + eb; }
 };
 
@@ -431,13 +449,14 @@ __device__ __forceinline__ void merge_thread(int s, const Ld& ld, Cmp cmp, const
 // Produces outputs [diag, diag + m) of the stable merge of A (byte address a0,
 // na keys) and B (b0, nb keys), where 0 < m <= ITEMS and diag + m <= na + nb:
 // the window never crosses the end of its pair, so every thread of a warp runs
-// the same code.  NS independent streams of H = ceil(ITEMS/NS) outputs keep NS
+// the same code.  `lanes` is the mask of the warp's lanes that make this call
+// (all of them reach it).  NS independent streams of H = ceil(ITEMS/NS) outputs keep NS
 // dependency chains in flight; stream s's merge-path search scans only the H+1
 // candidates after stream s-1's co-rank.  Outputs at or past m are computed
 // from in-bounds slack and dropped, never emitted.
-template <int ITEMS, class KeyT, int NS = 2, class Ld, class Cmp, class Emit>
+template <int ITEMS, class KeyT, int NS = 2, bool INNER = true, class Ld, class Cmp, class Emit>
 __device__ __forceinline__ void merge_window(const Ld& ld, Cmp cmp, uint32_t A0, int na, uint32_t B0, int nb, int diag,
-                                             int m, const Emit& emit) {
+                                             int m, unsigned lanes, const Emit& emit) {
   constexpr int H = (ITEMS + NS - 1) / NS;
   constexpr uint32_t S = sizeof(KeyT);
   if constexpr (NS == 2) {
@@ -452,17 +471,39 @@ __device__ __forceinline__ void merge_window(const Ld& ld, Cmp cmp, uint32_t A0,
     MergeCursor<KeyT> c1, c2;
     c1.init(ld, A0 + (uint32_t)ia1 * S, EA, B0 + (uint32_t)(diag - ia1) * S, EB);
     c2.init(ld, A0 + (uint32_t)ia2 * S, EA, B0 + (uint32_t)(d2 - ia2) * S, EB);
+    // INNER: when no calling lane of the warp can reach a run end within its
+    // window and every window is full, the lanes run the steps without end
+    // checks or emit predicates (a choice uniform over `lanes`, the mask of
+    // the warp's lanes that call this function, so no divergence).
+    const bool inner = m == ITEMS && na - ia1 >= H && nb - (diag - ia1) >= H && na - ia2 >= ITEMS - H &&
+                       nb - (d2 - ia2) >= ITEMS - H;
+    if (INNER && __all_sync(lanes, inner)) {
 #pragma unroll
-    for (int i = 0; i < H; ++i) {
-      uint32_t src1;
-      bool ta1;
-      const KeyT o1 = c1.step(ld, cmp, src1, ta1);
-      if (i < m) emit(i, o1, src1, ta1);
-      if (H + i < ITEMS) {
-        uint32_t src2;
-        bool ta2;
-        const KeyT o2 = c2.step(ld, cmp, src2, ta2);
-        if (H + i < m) emit(H + i, o2, src2, ta2);
+      for (int i = 0; i < H; ++i) {
+        uint32_t src1;
+        bool ta1;
+        const KeyT o1 = c1.step_inner(ld, cmp, src1, ta1);
+        emit(i, o1, src1, ta1);
+        if (H + i < ITEMS) {
+          uint32_t src2;
+          bool ta2;
+          const KeyT o2 = c2.step_inner(ld, cmp, src2, ta2);
+          emit(H + i, o2, src2, ta2);
+        }
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < H; ++i) {
+        uint32_t src1;
+        bool ta1;
+        const KeyT o1 = c1.step(ld, cmp, src1, ta1);
+        if (i < m) emit(i, o1, src1, ta1);
+        if (H + i < ITEMS) {
+          uint32_t src2;
+          bool ta2;
+          const KeyT o2 = c2.step(ld, cmp, src2, ta2);
+          if (H + i < m) emit(H + i, o2, src2, ta2);
+        }
       }
     }
   } else {

@@ -417,6 +417,7 @@ __global__ void __launch_bounds__(NT) base_warp_kernel(TileArgs<KeyT, NoVal> a) 
     const int tpp = (2 * rl + ITEMS_M - 1) / ITEMS_M;
     const KeyT* xk = cur ? k1 : k0;
     KeyT* yk = cur ? k0 : k1;
+    const unsigned lanes = __ballot_sync(0xffffffffu, tid < tpp * (TILE / (2 * rl)));
     if (tid < tpp * (TILE / (2 * rl))) {
       const int p = tid / tpp;
       const int diag = (tid - p * tpp) * ITEMS_M;
@@ -424,8 +425,8 @@ __global__ void __launch_bounds__(NT) base_warp_kernel(TileArgs<KeyT, NoVal> a) 
       const int m = min(ITEMS_M, 2 * rl - diag);
       const PlainLoad<KeyT> ld(xk);
       const SmemArray<KeyT> yka(yk + ps + diag);
-      merge_window<ITEMS_M, KeyT, 2>(ld, cmp, ld.addr(ps), rl, ld.addr(ps + rl), rl, diag, m,
-                                  [&](int i, KeyT k, uint32_t, bool) { yka.put(i, k); });
+      merge_window<ITEMS_M, KeyT, 2, false>(ld, cmp, ld.addr(ps), rl, ld.addr(ps + rl), rl, diag, m, lanes,
+                                     [&](int i, KeyT k, uint32_t, bool) { yka.put(i, k); });
     }
     __syncthreads();
     cur ^= 1;
@@ -688,6 +689,7 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
   for (int lev = 0, span = 2; lev == 0 || (span >> 1) < nk; ++lev, span <<= 1) {
     const int np = (nk + span - 1) / span;
     const int* wt = wst + lev * 17;
+    const unsigned lanes = __ballot_sync(0xffffffffu, tid < wt[np]);
     if (tid < wt[np]) {
       int p = 0;  // the last pair whose first window thread is <= tid
 #pragma unroll
@@ -709,7 +711,7 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
         const SmemArray<V> yva(v1 + ps + diag);
         const SmemArray<V> sva(reinterpret_cast<const V*>(stage_v));
         const int gen = a.gen_index;
-        merge_window<ITEMS, KeyT, NS>(ld, cmp, A0, na, B0, nb, diag, m, [&](int i, KeyT k, uint32_t src, bool ta) {
+        merge_window<ITEMS, KeyT, NS>(ld, cmp, A0, na, B0, nb, diag, m, lanes, [&](int i, KeyT k, uint32_t src, bool ta) {
           yka.put(i, k);
           if constexpr (kHasVal) {
             const int seg = ta ? si : si + 1;
@@ -725,8 +727,8 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
         const PlainLoad<KeyT> ld(xk);
         const SmemArray<KeyT> yka(yk + ps + diag);
         const SmemArray<V> xva(xv), yva(yv + ps + diag);
-        merge_window<ITEMS, KeyT, NS>(ld, cmp, ld.addr(ps), na, ld.addr(pm), nb, diag, m,
-                                  [&](int i, KeyT k, uint32_t src, bool) {
+        merge_window<ITEMS, KeyT, NS>(ld, cmp, ld.addr(ps), na, ld.addr(pm), nb, diag, m, lanes,
+                                      [&](int i, KeyT k, uint32_t src, bool) {
                                     yka.put(i, k);
                                     if constexpr (kHasVal)
                                       yva.put(i, xva.get((int)((src - ld.base) / (uint32_t)sizeof(KeyT))));
