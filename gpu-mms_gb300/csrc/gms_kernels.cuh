@@ -521,65 +521,50 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
   __syncthreads();
 
   // ---- warp 0: place the segments and issue their copies ----
+  // Ordered to start the copies early: the descriptor and output-offset loads
+  // go out together, the two prefix sums that place the segments run side by
+  // side, and the bookkeeping the merge levels need (segment starts, window
+  // tables) is written while the copies are in flight.
   if (tid < 32) {
     const int64_t gbase = g * a.L * a.k;
     const int64_t row = g * (a.tiles_full + 1) + j;
     const int64_t ng = min64(a.L * a.k, a.n - gbase);
     const uint64_t arr_k_lo = reinterpret_cast<uint64_t>(a.in);
     const uint64_t arr_k_hi = arr_k_lo + (uint64_t)a.n * sizeof(KeyT);
+    int64_t lo = 0, hi = 0;
+    if (lane < nk) {
+      lo = a.desc[row * nk + lane];
+      hi = a.desc[(row + 1) * nk + lane];
+    }
+    const int64_t out_off = (lane == 0) ? a.doff[row] : 0;
     int len = 0;
     int64_t gs = 0;
     bool bad = false;
     if (lane < nk) {
-      const int64_t lo = a.desc[row * nk + lane];
-      const int64_t hi = a.desc[(row + 1) * nk + lane];
       const int64_t rl = min64(a.L, ng - min64((int64_t)lane * a.L, ng));
       bad = !((lo >= 0) && (hi >= lo) && (hi <= rl) && (hi - lo <= TILE_MAX));
       len = bad ? 0 : (int)(hi - lo);
       gs = gbase + (int64_t)lane * a.L + (bad ? 0 : lo);
-    }
-    int incl = len;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += y;
-    }
-    const int total = __shfl_sync(0xffffffffu, incl, 31);
-    const bool any_bad = __any_sync(0xffffffffu, bad) || total > TILE_MAX;
-    if (lane < nk) cpre[lane + 1] = incl;
-    if (lane == 0) cpre[0] = 0;
-    // window table of every level: pair p of a level with `span` segments
-    // holds keys [cpre[p*span], cpre[min(p*span+span, nk)]) and gets
-    // ceil(len/ITEMS) threads starting at wst[lev*17 + p]
-    for (int lev = 0, span = 2; lev < Lay::kLevels && (lev == 0 || (span >> 1) < nk); ++lev, span <<= 1) {
-      const int np = (nk + span - 1) / span;
-      const int si = lane * span;
-      const int ei = min(si + span, nk);
-      const int ps = __shfl_sync(0xffffffffu, incl, max(min(si, nk) - 1, 0));
-      const int pe = __shfl_sync(0xffffffffu, incl, max(ei - 1, 0));
-      const int len = (lane < np) ? (si == 0 ? pe : pe - ps) : 0;
-      const int tcount = (len + ITEMS - 1) / ITEMS;
-      int tincl = tcount;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int y = __shfl_up_sync(0xffffffffu, tincl, o);
-        if (lane >= o) tincl += y;
-      }
-      if (lane < np) wst[lev * 17 + lane + 1] = tincl;
-      if (lane == 0) wst[lev * 17] = 0;
     }
     // key regions
     const uint64_t A = arr_k_lo + (uint64_t)gs * sizeof(KeyT);
     const uint64_t E = A + (uint64_t)len * sizeof(KeyT);
     const SegCopy ck = seg_copy(A, E, arr_k_lo, arr_k_hi);
     const uint32_t reg_k = (uint32_t)(ck.e16 - ck.a16);
+    int incl = len;
     uint32_t off_k = reg_k;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xffffffffu, off_k, o);
-      if (lane >= o) off_k += y;
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      const uint32_t z = __shfl_up_sync(0xffffffffu, off_k, o);
+      if (lane >= o) {
+        incl += y;
+        off_k += z;
+      }
     }
     off_k -= reg_k;  // exclusive
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    const bool any_bad = __any_sync(0xffffffffu, bad) || total > TILE_MAX;
     uint32_t bulk = (!any_bad && ck.be > ck.bs) ? (uint32_t)(ck.be - ck.bs) : 0u;
     SegCopy cv{};
     uint32_t off_v = 0;
@@ -606,18 +591,6 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
     uint32_t tx = bulk;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) tx += __shfl_xor_sync(0xffffffffu, tx, o);
-    if (lane < nk) {
-      sbk[lane] = (int)((off_k + (uint32_t)(A - ck.a16)) / sizeof(KeyT));
-      gsrc[lane] = gs;
-      if (carry) sbv[lane] = (int)((off_v + (uint32_t)(Av - cv.a16)) / sizeof(V));
-    }
-    if (lane == 0) {
-      meta[0] = gbase + a.doff[row];
-      meta[1] = gbase;
-      meta[2] = g;
-      meta[3] = any_bad ? -1 : total;
-      if (any_bad && a.err) atomicOr(a.err, DEV_BAD_SEGMENT);
-    }
     fence_proxy_async_smem();
     if (lane == 0) mbar_arrive_expect_tx(bar, tx);
     __syncwarp();
@@ -625,6 +598,12 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
       unsigned char* dstk = stage_k + off_k;
       if (ck.be > ck.bs) {
         bulk_g2s(dstk + (ck.bs - ck.a16), reinterpret_cast<const void*>(ck.bs), (uint32_t)(ck.be - ck.bs), bar);
+      }
+      if constexpr (kHasVal) {
+        if (carry && cv.be > cv.bs) {
+          unsigned char* dstv = stage_v + off_v;
+          bulk_g2s(dstv + (cv.bs - cv.a16), reinterpret_cast<const void*>(cv.bs), (uint32_t)(cv.be - cv.bs), bar);
+        }
       }
       // plain loads for bytes outside the array's 16-byte-aligned interior
       // (never more than 15 bytes at each end of the array)
@@ -641,9 +620,6 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
       if constexpr (kHasVal) {
         if (carry) {
           unsigned char* dstv = stage_v + off_v;
-          if (cv.be > cv.bs) {
-            bulk_g2s(dstv + (cv.bs - cv.a16), reinterpret_cast<const void*>(cv.bs), (uint32_t)(cv.be - cv.bs), bar);
-          }
           const V* vsrc = a.vin + gs;
           V* vdst = reinterpret_cast<V*>(dstv + (Av - cv.a16));
           for (int i = 0; i < len; ++i) {
@@ -656,6 +632,41 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
           }
         }
       }
+    }
+    // bookkeeping for the merge levels, written while the copies fly
+    if (lane < nk) {
+      cpre[lane + 1] = incl;
+      sbk[lane] = (int)((off_k + (uint32_t)(A - ck.a16)) / sizeof(KeyT));
+      gsrc[lane] = gs;
+      if (carry) sbv[lane] = (int)((off_v + (uint32_t)(Av - cv.a16)) / sizeof(V));
+    }
+    if (lane == 0) {
+      cpre[0] = 0;
+      meta[0] = gbase + out_off;
+      meta[1] = gbase;
+      meta[2] = g;
+      meta[3] = any_bad ? -1 : total;
+      if (any_bad && a.err) atomicOr(a.err, DEV_BAD_SEGMENT);
+    }
+    // window table of every level: pair p of a level with `span` segments
+    // holds keys [cpre[p*span], cpre[min(p*span+span, nk)]) and gets
+    // ceil(len/ITEMS) threads starting at wst[lev*17 + p]
+    for (int lev = 0, span = 2; lev < Lay::kLevels && (lev == 0 || (span >> 1) < nk); ++lev, span <<= 1) {
+      const int np = (nk + span - 1) / span;
+      const int si = lane * span;
+      const int ei = min(si + span, nk);
+      const int ps = __shfl_sync(0xffffffffu, incl, max(min(si, nk) - 1, 0));
+      const int pe = __shfl_sync(0xffffffffu, incl, max(ei - 1, 0));
+      const int plen = (lane < np) ? (si == 0 ? pe : pe - ps) : 0;
+      const int tcount = (plen + ITEMS - 1) / ITEMS;
+      int tincl = tcount;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, tincl, o);
+        if (lane >= o) tincl += y;
+      }
+      if (lane < np) wst[lev * 17 + lane + 1] = tincl;
+      if (lane == 0) wst[lev * 17] = 0;
     }
   }
 
