@@ -144,7 +144,7 @@ int load_cache(const char* path) {
     gms::Tune t;
     t.k = (int)k;
     t.sample_b = (int)sb;
-    t.bulk_copy = bulk != 0 ? 1 : 0;
+    t.bulk_copy = bulk < 0 || bulk > 2 ? 1 : (int)bulk;
     got.push_back(TuneEntry{(int)dt, (int)kv, (int)cls, t, ms});
     pos = b + 1;
   }
@@ -259,7 +259,7 @@ int gms_set_tune(int k, int sample_b, int bulk_copy) {
   std::lock_guard<std::mutex> g(g_tune_mu);
   g_tune.k = k;
   g_tune.sample_b = sample_b;
-  g_tune.bulk_copy = bulk_copy ? 1 : 0;
+  g_tune.bulk_copy = bulk_copy < 0 ? 0 : (bulk_copy > 2 ? 1 : bulk_copy);
   g_tune_explicit = true;
   return GMS_OK;
 }
@@ -321,7 +321,7 @@ int gms_autotune(int dtype, int kv, int64_t n, void* stream, int* out_k, int* ou
   } else {
     for (int k : {32, 16, 8})
       for (int sb : {32, 16, 64})
-        for (int bulk : {1, 0}) {
+        for (int bulk : {1, 2, 0}) {
           if (!valid_tune(k, sb)) continue;
           gms::Tune t;
           t.k = k;

@@ -483,7 +483,11 @@ struct WindowCap {
   static constexpr int value = (NT - 16) * ITEMS;
 };
 
-template <class KeyT, class V, class Cmp, class Codec, int NT, int ITEMS, int NS>
+// COPY selects how a tile's segments reach shared memory: 1 = warp 0 issues
+// one cp.async.bulk per segment (mbarrier completion); 2 = every warp
+// computes the placement and copies a share of the segments with 16-byte
+// cp.async (group completion), which spreads the issue over all warps.
+template <class KeyT, class V, class Cmp, class Codec, int NT, int ITEMS, int NS, int COPY = 1>
 __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, int64_t total_tiles) {
   constexpr int CAP = NT * ITEMS;                        // shared-memory buffers
   constexpr int TILE_MAX = WindowCap<NT, ITEMS>::value;  // keys a tile may hold
@@ -516,16 +520,19 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
   const int64_t jg = (g == a.groups - 1) ? a.tiles_last : a.tiles_full;
   if (j >= jg) return;
 
-  if (tid == 0) mbar_init(bar, 1);
-  fence_mbar_init();
-  __syncthreads();
+  if constexpr (COPY == 1) {
+    if (tid == 0) mbar_init(bar, 1);
+    fence_mbar_init();
+    __syncthreads();
+  }
 
   // ---- warp 0: place the segments and issue their copies ----
   // Ordered to start the copies early: the descriptor and output-offset loads
   // go out together, the two prefix sums that place the segments run side by
   // side, and the bookkeeping the merge levels need (segment starts, window
   // tables) is written while the copies are in flight.
-  if (tid < 32) {
+  const int warp = tid >> 5;
+  if (COPY == 2 || tid < 32) {
     const int64_t gbase = g * a.L * a.k;
     const int64_t row = g * (a.tiles_full + 1) + j;
     const int64_t ng = min64(a.L * a.k, a.n - gbase);
@@ -588,23 +595,54 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
         if (!any_bad && cv.be > cv.bs) bulk += (uint32_t)(cv.be - cv.bs);
       }
     }
-    uint32_t tx = bulk;
+    if constexpr (COPY == 1) {
+      uint32_t tx = bulk;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) tx += __shfl_xor_sync(0xffffffffu, tx, o);
-    fence_proxy_async_smem();
-    if (lane == 0) mbar_arrive_expect_tx(bar, tx);
-    __syncwarp();
-    if (!any_bad && lane < nk && len > 0) {
-      unsigned char* dstk = stage_k + off_k;
-      if (ck.be > ck.bs) {
-        bulk_g2s(dstk + (ck.bs - ck.a16), reinterpret_cast<const void*>(ck.bs), (uint32_t)(ck.be - ck.bs), bar);
-      }
-      if constexpr (kHasVal) {
-        if (carry && cv.be > cv.bs) {
-          unsigned char* dstv = stage_v + off_v;
-          bulk_g2s(dstv + (cv.bs - cv.a16), reinterpret_cast<const void*>(cv.bs), (uint32_t)(cv.be - cv.bs), bar);
+      for (int o = 16; o > 0; o >>= 1) tx += __shfl_xor_sync(0xffffffffu, tx, o);
+      fence_proxy_async_smem();
+      if (lane == 0) mbar_arrive_expect_tx(bar, tx);
+      __syncwarp();
+      if (!any_bad && lane < nk && len > 0) {
+        if (ck.be > ck.bs) {
+          bulk_g2s(stage_k + off_k + (ck.bs - ck.a16), reinterpret_cast<const void*>(ck.bs), (uint32_t)(ck.be - ck.bs),
+                   bar);
+        }
+        if constexpr (kHasVal) {
+          if (carry && cv.be > cv.bs) {
+            bulk_g2s(stage_v + off_v + (cv.bs - cv.a16), reinterpret_cast<const void*>(cv.bs),
+                     (uint32_t)(cv.be - cv.bs), bar);
+          }
         }
       }
+    } else {
+      // segment s goes to warp s % (NT/32); its lanes copy 16-byte chunks
+      (void)bulk;
+      if (!any_bad) {
+        for (int sg = warp; sg < nk; sg += NT / 32) {
+          const uint64_t bs = __shfl_sync(0xffffffffu, ck.bs, sg);
+          const uint64_t be = __shfl_sync(0xffffffffu, ck.be, sg);
+          const uint64_t a16 = __shfl_sync(0xffffffffu, ck.a16, sg);
+          const uint32_t ok = __shfl_sync(0xffffffffu, off_k, sg);
+          const int nch = be > bs ? (int)((be - bs) >> 4) : 0;
+          unsigned char* dst = stage_k + ok + (uint32_t)(bs - a16);
+          for (int c = lane; c < nch; c += 32) cp_async16(dst + 16 * c, reinterpret_cast<const void*>(bs + 16ull * c));
+          if constexpr (kHasVal) {
+            if (carry) {
+              const uint64_t vbs = __shfl_sync(0xffffffffu, cv.bs, sg);
+              const uint64_t vbe = __shfl_sync(0xffffffffu, cv.be, sg);
+              const uint64_t va16 = __shfl_sync(0xffffffffu, cv.a16, sg);
+              const uint32_t ov = __shfl_sync(0xffffffffu, off_v, sg);
+              const int nvc = vbe > vbs ? (int)((vbe - vbs) >> 4) : 0;
+              unsigned char* vdst = stage_v + ov + (uint32_t)(vbs - va16);
+              for (int c = lane; c < nvc; c += 32)
+                cp_async16(vdst + 16 * c, reinterpret_cast<const void*>(vbs + 16ull * c));
+            }
+          }
+        }
+      }
+    }
+    if (warp == 0 && !any_bad && lane < nk && len > 0) {
+      unsigned char* dstk = stage_k + off_k;
       // plain loads for bytes outside the array's 16-byte-aligned interior
       // (never more than 15 bytes at each end of the array)
       const KeyT* src = a.in + gs;
@@ -634,13 +672,13 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
       }
     }
     // bookkeeping for the merge levels, written while the copies fly
-    if (lane < nk) {
+    if (warp == 0 && lane < nk) {
       cpre[lane + 1] = incl;
       sbk[lane] = (int)((off_k + (uint32_t)(A - ck.a16)) / sizeof(KeyT));
       gsrc[lane] = gs;
       if (carry) sbv[lane] = (int)((off_v + (uint32_t)(Av - cv.a16)) / sizeof(V));
     }
-    if (lane == 0) {
+    if (tid == 0) {
       cpre[0] = 0;
       meta[0] = gbase + out_off;
       meta[1] = gbase;
@@ -665,8 +703,8 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
         const int y = __shfl_up_sync(0xffffffffu, tincl, o);
         if (lane >= o) tincl += y;
       }
-      if (lane < np) wst[lev * 17 + lane + 1] = tincl;
-      if (lane == 0) wst[lev * 17] = 0;
+      if (warp == 0 && lane < np) wst[lev * 17 + lane + 1] = tincl;
+      if (tid == 0) wst[lev * 17] = 0;
     }
   }
 
@@ -676,13 +714,18 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
   // bytes (and its own plain stores) before every other thread's reads.
   constexpr uint32_t kSpinLimit = 1u << 26;
   int* timed_out = cpre + 97;  // the padding word after the descriptors
-  if (tid < 32) {
-    const bool ok = mbar_wait_bounded(bar, 0, kSpinLimit);
-    if (lane == 0) *timed_out = ok ? 0 : 1;
-    if (!ok) {
-      if (lane == 0 && a.err) atomicOr(a.err, DEV_COPY_TIMEOUT);
-      mbar_wait_bounded(bar, 0, kSpinLimit);  // let copies in flight land
+  if constexpr (COPY == 1) {
+    if (tid < 32) {
+      const bool ok = mbar_wait_bounded(bar, 0, kSpinLimit);
+      if (lane == 0) *timed_out = ok ? 0 : 1;
+      if (!ok) {
+        if (lane == 0 && a.err) atomicOr(a.err, DEV_COPY_TIMEOUT);
+        mbar_wait_bounded(bar, 0, kSpinLimit);  // let copies in flight land
+      }
     }
+  } else {
+    cp_async_wait_all();
+    if (tid == 0) *timed_out = 0;
   }
   __syncthreads();
   if (*timed_out) return;

@@ -65,7 +65,7 @@ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 struct Tune {
   int k = 32;         // fan-in per round (<= 32)
   int sample_b = 32;  // block size of the forecast sample
-  int bulk_copy = 1;  // 1: merge with bulk-copy staging of the tile segments; 0: merge with plain loads
+  int bulk_copy = 1;  // tile staging: 1 cp.async.bulk by one warp; 2 cp.async by every warp; 0 plain loads
 };
 
 // Scratch layout, computed by a dry run of the same recursion as the real run.
@@ -358,12 +358,13 @@ struct Engine {
   // Launches blocks for tiles [a.tile_base, a.tile_base + grid) of a round
   // with `total_tiles` tiles (grid defaults to all of them).
   static cudaError_t launch_merge_tiles(const TileArgs<KeyT, VV>& a, int64_t total_tiles, cudaStream_t st,
-                                        int level, int64_t grid = -1) {
+                                        int level, int copy_mode, int64_t grid = -1) {
     if (grid < 0) grid = total_tiles - a.tile_base;
     if (grid <= 0) return cudaSuccess;
     if (grid > 0x7fffffff) return cudaErrorInvalidConfiguration;
     using GG = Geo<VV>;
-    auto kern = merge_tiles_kernel<KeyT, VV, Cmp, Codec, GG::NT, GG::ITEMS, GG::NS>;
+    auto kern = copy_mode == 2 ? merge_tiles_kernel<KeyT, VV, Cmp, Codec, GG::NT, GG::ITEMS, GG::NS, 2>
+                               : merge_tiles_kernel<KeyT, VV, Cmp, Codec, GG::NT, GG::ITEMS, GG::NS, 1>;
     const size_t smem = MergeSmemLayout<KeyT, VV, GG::CAP>::bytes;
     cudaError_t e = ensure_smem((const void*)kern, smem);
     if (e != cudaSuccess) return e;
@@ -452,14 +453,14 @@ struct Engine {
         const int64_t t1 = std::min(tiles_last, t0 + per);
         TileArgs<KeyT, VV> b = a;
         b.tile_base = t0;
-        e = launch_merge_tiles(b, t1, st, level, t1 - t0);
+        e = launch_merge_tiles(b, t1, st, level, t.bulk_copy, t1 - t0);
         if (e != cudaSuccess) return e;
         const int64_t safe = (t1 == tiles_last) ? n : std::max<int64_t>(0, (t1 * G - k) * (int64_t)sb);
         split->after(split->ctx, std::min(safe, n), st);
       }
       return cudaSuccess;
     }
-    if (t.bulk_copy) return launch_merge_tiles(a, groups * tiles_full, st, level);
+    if (t.bulk_copy) return launch_merge_tiles(a, groups * tiles_full, st, level, t.bulk_copy);
     return launch_tile<MODE_TILE>(a, groups * tiles_full, st, level);
   }
 

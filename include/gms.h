@@ -301,8 +301,10 @@ int gms_timing_reset(void);
  *              smallest merge-tile capacity of the prebuilt engines).  A sort whose sample
  *              recursion would get too deep for the tuning returns
  *              GMS_ERR_INVALID.
- *   bulk_copy  1: merge kernel staging each tile's segments in shared memory
- *              with cp.async.bulk (default); 0: merge with plain loads
+ *   bulk_copy  how the merge kernel stages a tile's segments in shared
+ *              memory: 1 one cp.async.bulk per segment issued by one warp
+ *              (default); 2 16-byte cp.async issued by every warp; 0 a merge
+ *              kernel with plain loads
  * A tuning set here applies to every dtype and size until gms_clear_tune,
  * which returns to the defaults and to the autotuned table below.
  * ------------------------------------------------------------------------- */
@@ -315,7 +317,7 @@ int gms_clear_tune(void);
  * the reference fixes K/PIPELINE/BLOCKS at compile time (src/params.h:18-20).
  *
  * gms_autotune times every candidate tuning (k in {8,16,32}, sample_b in
- * {16,32,64}, both merge paths) on a sort of n synthetic keys of `dtype`
+ * {16,32,64}, the three staging modes) on a sort of n synthetic keys of `dtype`
  * (0 i32, 1 u32, 2 f32, 3 i64, 4 u64, 5 f64; kv=1: with int32 values) on
  * `stream`, checks that all tunings give the same bits, and records the
  * fastest (median of repeats) for the size class floor(log2 n).  Later sorts
