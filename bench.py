@@ -115,11 +115,12 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows), "power_w_max": max(pw) if pw else None}
 
 
-def cpu_baseline(orc, n_sample, reps=3):
-    """std::sort, libstdc++ parallel mode, every host thread, on n_sample keys."""
+def cpu_baseline(orc, n_sample, reps=3, threads=None):
+    """std::sort, libstdc++ parallel mode, every host thread (or `threads`), on
+    n_sample keys."""
     import numpy as np
 
-    threads = os.cpu_count() or 1
+    threads = threads or os.cpu_count() or 1
     a = orc.gen_i32(n_sample, 0, SEED)
     best = None
     for _ in range(reps):
@@ -650,6 +651,7 @@ def run_ours(args):
     }
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(orc, min(n, 1 << 26))
+        line["cpu_baseline_1thread"] = cpu_baseline(orc, min(n, 1 << 24), reps=1, threads=1)
     if not args.no_extra:
         del inputs
         torch.cuda.empty_cache()
