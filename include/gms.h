@@ -306,7 +306,9 @@ int gms_timing_reset(void);
  *              (default); 2 16-byte cp.async issued by every warp; 0 a merge
  *              kernel with plain loads
  * A tuning set here applies to every dtype and size until gms_clear_tune,
- * which returns to the defaults and to the autotuned table below.
+ * which returns to the autotuned table below and, for classes it does not
+ * hold, the built-in defaults (k 32, sample_b 32, bulk_copy 1; bulk_copy 2
+ * for 64-bit keys with a payload).
  * ------------------------------------------------------------------------- */
 int gms_set_tune(int k, int sample_b, int bulk_copy);
 int gms_get_tune(int* k, int* sample_b, int* bulk_copy);
