@@ -357,3 +357,38 @@ def test_host_sort_pipelined(gms, oracle):
     assert lib.gms_sort_host_i32_async(hb.data_ptr(), ob.data_ptr(), big.size, st) == 0
     assert lib.gms_host_sync(st) == 0
     assert np.array_equal(ob.numpy(), oracle.sort(big))
+
+
+# Beyond 2^31 keys (64-bit sizes and offsets everywhere): at this size the
+# result is checked through size-independent properties -- sortedness, and the
+# multiset through order-independent sums -- rather than against the oracle.
+def test_sort_i32_beyond_2p31_properties(gms):
+    lib = gms.load()
+    n = (1 << 31) + 1001
+    free, _ = torch.cuda.mem_get_info()
+    if free < 24 * (1 << 30):
+        pytest.skip("needs ~24 GB of free device memory")
+    g = torch.Generator(device="cuda")
+    g.manual_seed(123)
+    keys = torch.randint(-(2**31), 2**31 - 1, (n,), dtype=torch.int32, device="cuda", generator=g)
+    keys[:: 1 << 20] = 2**31 - 1  # full range, heavy values at the ends
+    keys[7 :: 1 << 21] = -(2**31)
+
+    def sums(t):  # in chunks: a 2^31-element int64 temporary would need 17 GB
+        acc = [0, 0, 0]
+        for c in torch.split(t, 1 << 28):
+            x = c.to(torch.int64)
+            acc[0] += int(x.sum())
+            acc[1] += int(((x * x) % 1000000007).sum())
+            acc[2] += int((x * 2654435761 % 1000003).sum())
+        return tuple(acc)
+
+    before = sums(keys)
+    out = torch.empty_like(keys)
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assert lib.gms_sort_i32(keys.data_ptr(), out.data_ptr(), n, 0, st) == 0, lib.gms_last_error()
+    torch.cuda.synchronize()
+    assert gms.device_status() == 0
+    assert bool((out[1:] >= out[:-1]).all()), "not sorted"
+    assert sums(out) == before, "not a permutation of the input"
+    assert int(out[0]) == -(2**31) and int(out[-1]) == 2**31 - 1
