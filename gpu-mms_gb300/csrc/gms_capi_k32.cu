@@ -138,10 +138,15 @@ int host_sort_enqueue(const int32_t* host_in, int32_t* host_out, int64_t n, cuda
     e = cudaStreamWaitEvent(p->h2d, p->drained[slot], 0);
     if (e != cudaSuccess) return cuda_error(e, "cudaStreamWaitEvent");
   }
+  // Up to kChunks pieces of whole base tiles; a piece holds a multiple of k
+  // tiles when it can, so the first merge round also runs piece by piece.
   const int64_t tiles = gms::ceil_div(n, EngI32::BASE_TILE);
+  const int64_t fan = tune_for(0, 0, n).k;
+  int64_t per = gms::ceil_div(tiles, (int64_t)kChunks);
+  if (per >= fan) per = gms::ceil_div(per, fan) * fan;
   gms::BaseGate gate;
-  gate.chunks = (int)std::min<int64_t>(kChunks, tiles);
-  gate.tiles_per_chunk = gms::ceil_div(tiles, (int64_t)gate.chunks);
+  gate.tiles_per_chunk = per;
+  gate.chunks = (int)gms::ceil_div(tiles, per);
   gate.ready = p->ready[slot];
   for (int c = 0; c < gate.chunks; ++c) {
     const int64_t k0 = std::min(n, c * gate.tiles_per_chunk * EngI32::BASE_TILE);

@@ -487,6 +487,7 @@ struct Engine {
     const int P = passes_for(n, t.k);
     KeyT* buf[2] = {d0, d1};
     V* vbuf[2] = {vd0, vd1};
+    int rounds_done = 0;  // rounds already run chunk by chunk
     {
       TileArgs<KeyT, V> a{};
       a.in = src;
@@ -510,6 +511,12 @@ struct Engine {
         if (!gate) {
           e = launch_base_warp(a, tiles, st);
         } else {
+          // Host-fed: each chunk is sorted as far as it can be on its own --
+          // the base case and every round but the last whose groups fit whole
+          // inside a chunk -- as soon as its copy lands.
+          const int64_t ck = gate->tiles_per_chunk * BASE_TILE;
+          int pc = 0;
+          for (int64_t L = BASE_TILE; pc < P - 1 && ck % (L * t.k) == 0; L *= t.k) ++pc;
           for (int c = 0; c < gate->chunks && e == cudaSuccess; ++c) {
             const int64_t t0 = c * gate->tiles_per_chunk;
             if (t0 >= tiles) break;
@@ -517,12 +524,27 @@ struct Engine {
             e = cudaStreamWaitEvent(st, gate->ready[c], 0);
             if (e != cudaSuccess) break;
             TileArgs<KeyT, V> b = a;
-            b.in = a.in + t0 * BASE_TILE;
-            b.out = a.out + t0 * BASE_TILE;
-            b.n = std::min(n, t1 * BASE_TILE) - t0 * BASE_TILE;
+            const int64_t off = t0 * BASE_TILE;
+            const int64_t nc = std::min(n, t1 * BASE_TILE) - off;
+            b.in = a.in + off;
+            b.out = a.out + off;
+            b.n = nc;
             b.sample_out = a.sample_out ? a.sample_out + t0 * a.sample_run_len : nullptr;
             e = launch_base_warp(b, t1 - t0, st);
+            int cc = 0, sb = 0;
+            int64_t L = BASE_TILE;
+            for (int p = 0; p < pc && e == cudaSuccess; ++p) {
+              const int64_t lk = L * t.k;
+              const KeyT* sin = w.s1[sb] + (off / L) * ceil_div(L, t.sample_b);
+              KeyT* sout = w.s1[sb ^ 1] + (off / lk) * ceil_div(lk, t.sample_b);
+              e = round<V>(w, 0, buf[cc] + off, vbuf[cc] ? vbuf[cc] + off : nullptr, buf[cc ^ 1] + off,
+                           vbuf[cc ^ 1] ? vbuf[cc ^ 1] + off : nullptr, nc, L, t, sin, sout, 0, 0, 0, st);
+              cc ^= 1;
+              sb ^= 1;
+              L = lk;
+            }
           }
+          rounds_done = pc;
         }
       } else {
         for (int c = 0; gate && c < gate->chunks && e == cudaSuccess; ++c) e = cudaStreamWaitEvent(st, gate->ready[c], 0);
@@ -530,10 +552,11 @@ struct Engine {
       }
       if (e != cudaSuccess) return e;
     }
-    int cur = 0;
-    int sbuf = 0;
+    int cur = rounds_done & 1;
+    int sbuf = rounds_done & 1;
     int64_t L = BASE_TILE;
-    for (int p = 0; p < P; ++p) {
+    for (int p = 0; p < rounds_done; ++p) L *= t.k;
+    for (int p = rounds_done; p < P; ++p) {
       const bool last = (p == P - 1);
       KeyT* sout = last ? nullptr : w.s1[sbuf ^ 1];
       KeyT* o = last ? dst : buf[cur ^ 1];

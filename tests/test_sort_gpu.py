@@ -329,7 +329,8 @@ def test_sort_with_explicit_workspace(gms, oracle, dtype, kv):
 def test_host_sort_pipelined(gms, oracle):
     lib = gms.load()
     st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
-    for n in (1, 8191, 8193, 3 * 8192 + 5, 1_000_003):
+    # the last two sizes sort their first merge round piece by piece
+    for n in (1, 8191, 8193, 3 * 8192 + 5, 1_000_003, (1 << 22) + 12345, (1 << 25) + 5):
         a = oracle.gen_i32(n, 6, n)
         hin = torch.from_numpy(a).pin_memory()
         hout = torch.empty_like(hin).pin_memory()
