@@ -102,7 +102,10 @@ int pipe_for(cudaStream_t st, HostPipe** out) {
   return GMS_OK;
 }
 
-int host_sort_enqueue(const int32_t* host_in, int32_t* host_out, int64_t n, cudaStream_t st) {
+// early_rounds: run the early merge rounds piece by piece as the input lands
+// (worth it when nothing else overlaps the copies; a pipeline of calls
+// already overlaps them with the neighbouring sorts).
+int host_sort_enqueue(const int32_t* host_in, int32_t* host_out, int64_t n, cudaStream_t st, bool early_rounds) {
   clear_error();
   if (n < 0) return set_error(GMS_ERR_INVALID, "n < 0");
   if (n == 0) return GMS_OK;
@@ -148,6 +151,7 @@ int host_sort_enqueue(const int32_t* host_in, int32_t* host_out, int64_t n, cuda
   gate.tiles_per_chunk = per;
   gate.chunks = (int)gms::ceil_div(tiles, per);
   gate.ready = p->ready[slot];
+  gate.early_rounds = early_rounds;
   for (int c = 0; c < gate.chunks; ++c) {
     const int64_t k0 = std::min(n, c * gate.tiles_per_chunk * EngI32::BASE_TILE);
     const int64_t k1 = std::min(n, (c + 1) * gate.tiles_per_chunk * EngI32::BASE_TILE);
@@ -318,13 +322,13 @@ int gms_find_partitions_i32(const int32_t* task, int64_t size, int k, int64_t ta
 }
 
 int gms_sort_host_i32_async(const int32_t* host_in, int32_t* host_out, int64_t n, void* stv) {
-  return host_sort_enqueue(host_in, host_out, n, (cudaStream_t)stv);
+  return host_sort_enqueue(host_in, host_out, n, (cudaStream_t)stv, false);
 }
 
 int gms_host_sync(void* stv) { return host_sync((cudaStream_t)stv); }
 
 int gms_sort_host_i32(const int32_t* host_in, int32_t* host_out, int64_t n, void* stv) {
-  const int status = host_sort_enqueue(host_in, host_out, n, (cudaStream_t)stv);
+  const int status = host_sort_enqueue(host_in, host_out, n, (cudaStream_t)stv, true);
   if (status != GMS_OK) return status;
   return host_sync((cudaStream_t)stv);
 }

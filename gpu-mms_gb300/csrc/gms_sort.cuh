@@ -195,6 +195,7 @@ struct BaseGate {
   int chunks = 0;
   int64_t tiles_per_chunk = 0;
   const cudaEvent_t* ready = nullptr;
+  bool early_rounds = true;  // also run the merge rounds whose groups fit a chunk, chunk by chunk
 };
 
 // Last round in parts: the tile merge of a single-group round is launched in
@@ -516,7 +517,7 @@ struct Engine {
           // inside a chunk -- as soon as its copy lands.
           const int64_t ck = gate->tiles_per_chunk * BASE_TILE;
           int pc = 0;
-          for (int64_t L = BASE_TILE; pc < P - 1 && ck % (L * t.k) == 0; L *= t.k) ++pc;
+          for (int64_t L = BASE_TILE; gate->early_rounds && pc < P - 1 && ck % (L * t.k) == 0; L *= t.k) ++pc;
           for (int c = 0; c < gate->chunks && e == cudaSuccess; ++c) {
             const int64_t t0 = c * gate->tiles_per_chunk;
             if (t0 >= tiles) break;

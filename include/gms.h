@@ -124,7 +124,8 @@ int gms_sort_i32_noalloc(int32_t* input, int32_t* output, int64_t n, void* strea
  * ------------------------------------------------------------------------- */
 int gms_sort_host_i32(const int32_t* host_in, int32_t* host_out, int64_t n, void* stream);
 /* Pipelined form (no reference counterpart): enqueues the same copy-in, sort
- * and copy-out and returns at once; `host_out` holds the result, and `host_in`
+ * (early merge rounds on the whole array: the pipeline already overlaps the
+ * copies with the neighbouring sorts) and copy-out and returns at once; `host_out` holds the result, and `host_in`
  * may be reused, after gms_host_sync(stream).  Two calls can be in flight per
  * stream: the input copy of one call and the output copy of the one before it
  * overlap the sort of the other.  The input copy is not ordered after earlier
