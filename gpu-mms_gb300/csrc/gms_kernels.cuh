@@ -359,7 +359,8 @@ struct BaseWarpSmem {
   using Geo = BaseWarpGeom<NT, KPL, ITEMS_M>;
   static constexpr int SPAN = Geo::TILE + ITEMS_M;
   static constexpr size_t buf = ((sizeof(KeyT) * (SPAN + 4) + 15) / 16) * 16;
-  static constexpr size_t bytes = 2 * buf;
+  static constexpr size_t off_bar = 2 * buf;  // mbarrier of the tile's bulk load
+  static constexpr size_t bytes = off_bar + 16;
 };
 
 template <class KeyT, class Cmp, class Codec, int NT, int KPL, int ITEMS_M>
@@ -378,12 +379,42 @@ __global__ void __launch_bounds__(NT) base_warp_kernel(TileArgs<KeyT, NoVal> a) 
   if (base >= a.n) return;
   const int cnt = (int)min64(TILE, a.n - base);
 
-  // Coalesced striped load: register i of thread t holds element t + i*NT.
+  // Load: register i of thread t holds element t + i*NT.  A full tile at a
+  // 16-byte-aligned address arrives by one bulk copy (TMA) into the second
+  // buffer and is read from there (one copy engine request instead of KPL
+  // loads per thread); otherwise coalesced loads straight from global memory.
   KeyT x[KPL];
+  const bool bulk = cnt == TILE && (reinterpret_cast<uint64_t>(a.in + base) & 15) == 0;
+  if (bulk) {
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + BaseWarpSmem<KeyT, NT, KPL, ITEMS_M>::off_bar);
+    int* timed_out = reinterpret_cast<int*>(smem) + 0;  // k0[0], free until the warp runs are stored
+    if (tid == 0) {
+      mbar_init(bar, 1);
+      fence_mbar_init();
+      mbar_arrive_expect_tx(bar, (uint32_t)(TILE * sizeof(KeyT)));
+      bulk_g2s(k1, a.in + base, (uint32_t)(TILE * sizeof(KeyT)), bar);
+    }
+    if (tid < 32) {
+      constexpr uint32_t kSpinLimit = 1u << 26;
+      __syncwarp();
+      const bool ok = mbar_wait_bounded(bar, 0, kSpinLimit);
+      if (lane == 0) *timed_out = ok ? 0 : 1;
+      if (!ok) {
+        if (lane == 0 && a.err) atomicOr(a.err, DEV_COPY_TIMEOUT);
+        mbar_wait_bounded(bar, 0, kSpinLimit);  // let the copy in flight land
+      }
+    }
+    __syncthreads();
+    if (*timed_out) return;
 #pragma unroll
-  for (int i = 0; i < KPL; ++i) {
-    const int p = tid + i * NT;
-    if (p < cnt) x[i] = maybe_enc<Codec>(a.in[base + p], a.enc_on_load);
+    for (int i = 0; i < KPL; ++i) x[i] = maybe_enc<Codec>(k1[tid + i * NT], a.enc_on_load);
+    __syncthreads();  // k0[0] and k1 are reused below
+  } else {
+#pragma unroll
+    for (int i = 0; i < KPL; ++i) {
+      const int p = tid + i * NT;
+      if (p < cnt) x[i] = maybe_enc<Codec>(a.in[base + p], a.enc_on_load);
+    }
   }
   if (cnt < TILE) {
     // a short last tile is padded with copies of its largest key
@@ -758,21 +789,30 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
       const int m = min(ITEMS, pe - ps - diag);
       const int na = pm - ps, nb = pe - pm;
       if (lev == 0) {
-        const EncLoad<KeyT, Codec> ld(reinterpret_cast<const KeyT*>(stage_k), a.enc_on_load);
-        const uint32_t A0 = ld.addr(sbk[si]);
-        const uint32_t B0 = (si + 1 < nk) ? ld.addr(sbk[si + 1]) : A0 + (uint32_t)na * sizeof(KeyT);
-        const SmemArray<KeyT> yka(k1 + ps + diag);
-        const SmemArray<V> yva(v1 + ps + diag);
-        const SmemArray<V> sva(reinterpret_cast<const V*>(stage_v));
-        const int gen = a.gen_index;
-        merge_window<ITEMS, KeyT, NS>(ld, cmp, A0, na, B0, nb, diag, m, lanes, [&](int i, KeyT k, uint32_t src, bool ta) {
-          yka.put(i, k);
-          if constexpr (kHasVal) {
-            const int seg = ta ? si : si + 1;
-            const int off = (int)((src - ld.base) / (uint32_t)sizeof(KeyT)) - sbk[seg];
-            yva.put(i, gen ? (V)(gsrc[seg] + off) : sva.get(sbv[seg] + off));
-          }
-        });
+        // the staged keys are encoded while read only when the round's input
+        // is raw caller data (a uniform branch: two specialised loops)
+        auto level0 = [&](const auto& ld) {
+          const uint32_t A0 = ld.addr(sbk[si]);
+          const uint32_t B0 = (si + 1 < nk) ? ld.addr(sbk[si + 1]) : A0 + (uint32_t)na * sizeof(KeyT);
+          const SmemArray<KeyT> yka(k1 + ps + diag);
+          const SmemArray<V> yva(v1 + ps + diag);
+          const SmemArray<V> sva(reinterpret_cast<const V*>(stage_v));
+          const int gen = a.gen_index;
+          merge_window<ITEMS, KeyT, NS>(ld, cmp, A0, na, B0, nb, diag, m, lanes,
+                                        [&](int i, KeyT k, uint32_t src, bool ta) {
+                                          yka.put(i, k);
+                                          if constexpr (kHasVal) {
+                                            const int seg = ta ? si : si + 1;
+                                            const int off = (int)((src - ld.base) / (uint32_t)sizeof(KeyT)) - sbk[seg];
+                                            yva.put(i, gen ? (V)(gsrc[seg] + off) : sva.get(sbv[seg] + off));
+                                          }
+                                        });
+        };
+        if (a.enc_on_load) {
+          level0(EncLoad<KeyT, Codec>(reinterpret_cast<const KeyT*>(stage_k), 1));
+        } else {
+          level0(PlainLoad<KeyT>(reinterpret_cast<const KeyT*>(stage_k)));
+        }
       } else {
         const KeyT* xk = (cur ? k1 : k0);
         KeyT* yk = (cur ? k0 : k1);
