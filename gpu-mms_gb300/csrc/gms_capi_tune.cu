@@ -144,7 +144,7 @@ int load_cache(const char* path) {
     gms::Tune t;
     t.k = (int)k;
     t.sample_b = (int)sb;
-    t.bulk_copy = bulk < 0 || bulk > 2 ? 1 : (int)bulk;
+    t.bulk_copy = bulk < 0 || bulk > 3 ? 1 : (int)bulk;
     got.push_back(TuneEntry{(int)dt, (int)kv, (int)cls, t, ms});
     pos = b + 1;
   }
@@ -235,11 +235,14 @@ gms::Tune current_tune() {
 }
 
 // Built-in tuning of a class when neither gms_set_tune nor the autotuned
-// table says otherwise (timed on GB300): 64-bit keys with a payload stage
-// their tiles faster with 16-byte copies issued by every warp.
+// table says otherwise (timed on GB300, 2^27 keys): sorts with a payload
+// merge faster with persistent CTAs that stage the next tile while storing
+// the current one (float32 + int32 -2%, uint64 + int32 -4%); keys-only sorts
+// do not (+1%).
 gms::Tune builtin_tune(int dtype, int kv) {
+  (void)dtype;
   gms::Tune t;
-  if (kv && dtype >= 3) t.bulk_copy = 2;
+  if (kv) t.bulk_copy = 3;
   return t;
 }
 
@@ -268,7 +271,7 @@ int gms_set_tune(int k, int sample_b, int bulk_copy) {
   std::lock_guard<std::mutex> g(g_tune_mu);
   g_tune.k = k;
   g_tune.sample_b = sample_b;
-  g_tune.bulk_copy = bulk_copy < 0 ? 0 : (bulk_copy > 2 ? 1 : bulk_copy);
+  g_tune.bulk_copy = bulk_copy < 0 ? 0 : (bulk_copy > 3 ? 1 : bulk_copy);
   g_tune_explicit = true;
   return GMS_OK;
 }
@@ -330,7 +333,7 @@ int gms_autotune(int dtype, int kv, int64_t n, void* stream, int* out_k, int* ou
   } else {
     for (int k : {32, 16, 8})
       for (int sb : {32, 16, 64})
-        for (int bulk : {1, 2, 0}) {
+        for (int bulk : {1, 3, 2, 0}) {
           if (!valid_tune(k, sb)) continue;
           gms::Tune t;
           t.k = k;

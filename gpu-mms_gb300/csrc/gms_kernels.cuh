@@ -482,7 +482,7 @@ __global__ void __launch_bounds__(NT) base_warp_kernel(TileArgs<KeyT, NoVal> a) 
 // ping-pong between the merge buffer and the (now free) staging buffer.  Three
 // CTAs of 512 threads fit an SM for 4-byte keys, so one CTA's copy latency is
 // covered by the others' merging.
-template <class KeyT, class V, int CAP>
+template <class KeyT, class V, int CAP, int SETS = 1>
 struct MergeSmemLayout {
   static constexpr bool kHasVal = HasVal<V>::value;
   static constexpr int kMaxK = 32;
@@ -495,15 +495,17 @@ struct MergeSmemLayout {
   static constexpr size_t off_stage_v = stage_k_bytes;
   static constexpr size_t off_mk = off_stage_v + stage_v_bytes;
   static constexpr size_t off_mv = off_mk + mk_bytes;
-  static constexpr size_t off_desc = off_mv + mv_bytes;
-  // cpre[33] int, sbk[32] int, sbv[32] int, (pad), gsrc[32] int64, meta[4] int64, bar,
-  // wst[kLevels][17] int (first thread of each pair's windows, per level)
+  // SETS descriptor sets, one per tile in flight: cpre[33] int, sbk[32] int,
+  // sbv[32] int, a status word, gsrc[32] int64, meta[4] int64, wst[kLevels][17]
+  // int (first thread of each pair's windows, per level); then the mbarrier.
   static constexpr int kLevels = 5;  // log2(kMaxK)
-  static constexpr size_t off_gsrc = off_desc + 4 * (33 + 32 + 32) + 4;
-  static constexpr size_t off_meta = off_gsrc + 8 * 32;
-  static constexpr size_t off_bar = off_meta + 8 * 4;
-  static constexpr size_t off_wst = off_bar + 16;
-  static constexpr size_t bytes = off_wst + 4 * kLevels * 17;
+  static constexpr size_t set_gsrc = 400;
+  static constexpr size_t set_meta = set_gsrc + 8 * 32;
+  static constexpr size_t set_wst = set_meta + 8 * 4;
+  static constexpr size_t set_bytes = round16(set_wst + 4 * kLevels * 17);
+  static constexpr size_t off_desc = off_mv + mv_bytes;
+  static constexpr size_t off_bar = off_desc + SETS * set_bytes;
+  static constexpr size_t bytes = off_bar + 16;
 };
 
 // Merge-tile capacity with window-aligned levels: at a level with np pairs
@@ -514,17 +516,40 @@ struct WindowCap {
   static constexpr int value = (NT - 16) * ITEMS;
 };
 
+// One descriptor set in shared memory (see MergeSmemLayout).
+struct TileDesc {
+  int* cpre;      // segment prefix: segment s is keys [cpre[s], cpre[s+1]) of the tile
+  int* sbk;       // element index of segment s in the staged keys
+  int* sbv;       // ... in the staged payload
+  int* status;    // 1: the copy wait timed out
+  int64_t* gsrc;  // global index of segment s's first key
+  int64_t* meta;  // output offset, run base, run index, key count (-1: rejected)
+  int* wst;       // window tables
+  __device__ __forceinline__ TileDesc(unsigned char* base, size_t set_gsrc, size_t set_meta, size_t set_wst)
+      : cpre(reinterpret_cast<int*>(base)),
+        sbk(cpre + 33),
+        sbv(sbk + 32),
+        status(cpre + 97),
+        gsrc(reinterpret_cast<int64_t*>(base + set_gsrc)),
+        meta(reinterpret_cast<int64_t*>(base + set_meta)),
+        wst(reinterpret_cast<int*>(base + set_wst)) {}
+};
+
 // COPY selects how a tile's segments reach shared memory: 1 = warp 0 issues
 // one cp.async.bulk per segment (mbarrier completion); 2 = every warp
 // computes the placement and copies a share of the segments with 16-byte
 // cp.async (group completion), which spreads the issue over all warps.
-template <class KeyT, class V, class Cmp, class Codec, int NT, int ITEMS, int NS, int COPY = 1>
+// PERSIST (with COPY 1): each CTA loops over tiles blockIdx.x + i*gridDim.x;
+// when the merged tile ends in the merge buffer, warp 0 stages the next tile
+// into the free staging buffer while the other warps store the current one.
+template <class KeyT, class V, class Cmp, class Codec, int NT, int ITEMS, int NS, int COPY = 1, bool PERSIST = false>
 __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, int64_t total_tiles) {
+  static_assert(!PERSIST || COPY == 1, "persistent tiles stage with bulk copies");
   constexpr int CAP = NT * ITEMS;                        // shared-memory buffers
   constexpr int TILE_MAX = WindowCap<NT, ITEMS>::value;  // keys a tile may hold
   constexpr bool kHasVal = HasVal<V>::value;
-  using Lay = MergeSmemLayout<KeyT, V, CAP>;
-  static_assert(Lay::off_gsrc % 8 == 0, "descriptor alignment");
+  using Lay = MergeSmemLayout<KeyT, V, CAP, PERSIST ? 2 : 1>;
+  static_assert(Lay::off_desc % 16 == 0 && Lay::set_gsrc % 8 == 0, "descriptor alignment");
   extern __shared__ __align__(16) unsigned char smem[];
   unsigned char* stage_k = smem;
   unsigned char* stage_v = smem + Lay::off_stage_v;
@@ -532,24 +557,34 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
   KeyT* const k1 = reinterpret_cast<KeyT*>(smem + Lay::off_mk);
   V* const v0 = reinterpret_cast<V*>(stage_v);
   V* const v1 = reinterpret_cast<V*>(smem + Lay::off_mv);
-  int* cpre = reinterpret_cast<int*>(smem + Lay::off_desc);
-  int* sbk = cpre + 33;
-  int* sbv = sbk + 32;
-  int64_t* gsrc = reinterpret_cast<int64_t*>(smem + Lay::off_gsrc);
-  int64_t* meta = reinterpret_cast<int64_t*>(smem + Lay::off_meta);
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem + Lay::off_bar);
-  int* wst = reinterpret_cast<int*>(smem + Lay::off_wst);
   const Cmp cmp;
   const int tid = threadIdx.x;
   const int lane = tid & 31;
+  const int warp = tid >> 5;
   const int nk = a.k;
-
-  const int64_t tau = a.tile_base + blockIdx.x;
+  auto desc_set = [&](int s) {
+    return TileDesc(smem + Lay::off_desc + (size_t)s * Lay::set_bytes, Lay::set_gsrc, Lay::set_meta, Lay::set_wst);
+  };
+  // tiles of this launch: [a.tile_base, total_tiles); indices past a group's
+  // last tile are empty
+  auto real_tile = [&](int64_t t) {
+    const int64_t g = t / a.tiles_full;
+    const int64_t j = t - g * a.tiles_full;
+    return j < ((g == a.groups - 1) ? a.tiles_last : a.tiles_full);
+  };
+  auto next_tile = [&](int64_t t) {
+    if (!PERSIST) return total_tiles;
+    for (t += gridDim.x; t < total_tiles && !real_tile(t); t += gridDim.x) {
+    }
+    return t < total_tiles ? t : total_tiles;
+  };
+  int64_t tau = a.tile_base + blockIdx.x;
   if (tau >= total_tiles) return;
-  const int64_t g = tau / a.tiles_full;
-  const int64_t j = tau - g * a.tiles_full;
-  const int64_t jg = (g == a.groups - 1) ? a.tiles_last : a.tiles_full;
-  if (j >= jg) return;
+  if (!real_tile(tau)) {
+    tau = next_tile(tau);
+    if (tau >= total_tiles) return;
+  }
 
   if constexpr (COPY == 1) {
     if (tid == 0) mbar_init(bar, 1);
@@ -557,24 +592,35 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
     __syncthreads();
   }
 
-  // ---- warp 0: place the segments and issue their copies ----
-  // Ordered to start the copies early: the descriptor and output-offset loads
-  // go out together, the two prefix sums that place the segments run side by
-  // side, and the bookkeeping the merge levels need (segment starts, window
-  // tables) is written while the copies are in flight.
-  const int warp = tid >> 5;
-  if (COPY == 2 || tid < 32) {
+  // ---- place tile t's segments in the staging buffer and issue their copies
+  // (warp 0; every warp with COPY 2), filling descriptor set d.  Ordered to
+  // start the copies early: the descriptor and output-offset loads go out
+  // together, the two prefix sums that place the segments run side by side,
+  // and the bookkeeping the merge levels need (segment starts, window tables)
+  // is written while the copies are in flight.
+  // A tile's boundary row (lane s: run s's first and end offsets; lane 0 also
+  // the tile's output offset), loaded ahead of its use.
+  struct Bounds {
+    int64_t lo = 0, hi = 0, out_off = 0;
+  };
+  auto load_bounds = [&](int64_t t) {
+    Bounds b;
+    const int64_t g = t / a.tiles_full;
+    const int64_t row = g * (a.tiles_full + 1) + (t - g * a.tiles_full);
+    if (lane < nk) {
+      b.lo = a.desc[row * nk + lane];
+      b.hi = a.desc[(row + 1) * nk + lane];
+    }
+    if (lane == 0) b.out_off = a.doff[row];
+    return b;
+  };
+  auto stage = [&](int64_t t, const TileDesc& d, const Bounds& bd) {
+    const int64_t g = t / a.tiles_full;
     const int64_t gbase = g * a.L * a.k;
-    const int64_t row = g * (a.tiles_full + 1) + j;
     const int64_t ng = min64(a.L * a.k, a.n - gbase);
     const uint64_t arr_k_lo = reinterpret_cast<uint64_t>(a.in);
     const uint64_t arr_k_hi = arr_k_lo + (uint64_t)a.n * sizeof(KeyT);
-    int64_t lo = 0, hi = 0;
-    if (lane < nk) {
-      lo = a.desc[row * nk + lane];
-      hi = a.desc[(row + 1) * nk + lane];
-    }
-    const int64_t out_off = (lane == 0) ? a.doff[row] : 0;
+    const int64_t lo = bd.lo, hi = bd.hi, out_off = bd.out_off;
     int len = 0;
     int64_t gs = 0;
     bool bad = false;
@@ -704,17 +750,17 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
     }
     // bookkeeping for the merge levels, written while the copies fly
     if (warp == 0 && lane < nk) {
-      cpre[lane + 1] = incl;
-      sbk[lane] = (int)((off_k + (uint32_t)(A - ck.a16)) / sizeof(KeyT));
-      gsrc[lane] = gs;
-      if (carry) sbv[lane] = (int)((off_v + (uint32_t)(Av - cv.a16)) / sizeof(V));
+      d.cpre[lane + 1] = incl;
+      d.sbk[lane] = (int)((off_k + (uint32_t)(A - ck.a16)) / sizeof(KeyT));
+      d.gsrc[lane] = gs;
+      if (carry) d.sbv[lane] = (int)((off_v + (uint32_t)(Av - cv.a16)) / sizeof(V));
     }
-    if (tid == 0) {
-      cpre[0] = 0;
-      meta[0] = gbase + out_off;
-      meta[1] = gbase;
-      meta[2] = g;
-      meta[3] = any_bad ? -1 : total;
+    if (warp == 0 && lane == 0) {
+      d.cpre[0] = 0;
+      d.meta[0] = gbase + out_off;
+      d.meta[1] = gbase;
+      d.meta[2] = g;
+      d.meta[3] = any_bad ? -1 : total;
       if (any_bad && a.err) atomicOr(a.err, DEV_BAD_SEGMENT);
     }
     // window table of every level: pair p of a level with `span` segments
@@ -734,117 +780,148 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
         const int y = __shfl_up_sync(0xffffffffu, tincl, o);
         if (lane >= o) tincl += y;
       }
-      if (warp == 0 && lane < np) wst[lev * 17 + lane + 1] = tincl;
-      if (tid == 0) wst[lev * 17] = 0;
+      if (warp == 0 && lane < np) d.wst[lev * 17 + lane + 1] = tincl;
+      if (warp == 0 && lane == 0) d.wst[lev * 17] = 0;
     }
-  }
+  };
 
-  // ---- wait for the staged segments (bounded) ----
-  // Only warp 0 polls the mbarrier; the other warps wait in the block barrier,
-  // which issues nothing.  The barrier orders warp 0's acquire of the copied
-  // bytes (and its own plain stores) before every other thread's reads.
-  constexpr uint32_t kSpinLimit = 1u << 26;
-  int* timed_out = cpre + 97;  // the padding word after the descriptors
-  if constexpr (COPY == 1) {
-    if (tid < 32) {
-      const bool ok = mbar_wait_bounded(bar, 0, kSpinLimit);
-      if (lane == 0) *timed_out = ok ? 0 : 1;
-      if (!ok) {
-        if (lane == 0 && a.err) atomicOr(a.err, DEV_COPY_TIMEOUT);
-        mbar_wait_bounded(bar, 0, kSpinLimit);  // let copies in flight land
-      }
-    }
-  } else {
-    cp_async_wait_all();
-    if (tid == 0) *timed_out = 0;
-  }
-  __syncthreads();
-  if (*timed_out) return;
-  const int cnt = (int)meta[3];
-  if (cnt < 0) return;  // rejected tile (never expected): nothing was copied
-  const int64_t out_base = meta[0];
-  const int64_t run_base = meta[1];
-  const int64_t run_index = meta[2];
-
-  // ---- levels: window-aligned merges, pair by pair ----
-  // Level 0 merges staged segment pairs (2p, 2p+1) into the merge buffer; the
-  // later levels ping-pong between the merge buffer and the staging buffer,
-  // pair p of level `lev` merging the outputs of pairs 2p and 2p+1 below.
-  int cur = 0;  // 0: the staging buffer holds the current input
-  for (int lev = 0, span = 2; lev == 0 || (span >> 1) < nk; ++lev, span <<= 1) {
-    const int np = (nk + span - 1) / span;
-    const int* wt = wst + lev * 17;
-    const unsigned lanes = __ballot_sync(0xffffffffu, tid < wt[np]);
-    if (tid < wt[np]) {
-      int p = 0;  // the last pair whose first window thread is <= tid
-#pragma unroll
-      for (int step = 16; step > 0; step >>= 1) {
-        if (p + step < np && wt[p + step] <= tid) p += step;
-      }
-      const int si = p * span;
-      const int mi = min(si + (span >> 1), nk);
-      const int ei = min(si + span, nk);
-      const int ps = cpre[si], pm = cpre[mi], pe = cpre[ei];
-      const int diag = (tid - wt[p]) * ITEMS;
-      const int m = min(ITEMS, pe - ps - diag);
-      const int na = pm - ps, nb = pe - pm;
-      if (lev == 0) {
-        // the staged keys are encoded while read only when the round's input
-        // is raw caller data (a uniform branch: two specialised loops)
-        auto level0 = [&](const auto& ld) {
-          const uint32_t A0 = ld.addr(sbk[si]);
-          const uint32_t B0 = (si + 1 < nk) ? ld.addr(sbk[si + 1]) : A0 + (uint32_t)na * sizeof(KeyT);
-          const SmemArray<KeyT> yka(k1 + ps + diag);
-          const SmemArray<V> yva(v1 + ps + diag);
-          const SmemArray<V> sva(reinterpret_cast<const V*>(stage_v));
-          const int gen = a.gen_index;
-          merge_window<ITEMS, KeyT, NS>(ld, cmp, A0, na, B0, nb, diag, m, lanes,
-                                        [&](int i, KeyT k, uint32_t src, bool ta) {
-                                          yka.put(i, k);
-                                          if constexpr (kHasVal) {
-                                            const int seg = ta ? si : si + 1;
-                                            const int off = (int)((src - ld.base) / (uint32_t)sizeof(KeyT)) - sbk[seg];
-                                            yva.put(i, gen ? (V)(gsrc[seg] + off) : sva.get(sbv[seg] + off));
-                                          }
-                                        });
-        };
-        if (a.enc_on_load) {
-          level0(EncLoad<KeyT, Codec>(reinterpret_cast<const KeyT*>(stage_k), 1));
-        } else {
-          level0(PlainLoad<KeyT>(reinterpret_cast<const KeyT*>(stage_k)));
+  if (COPY == 2 || warp == 0) stage(tau, desc_set(0), load_bounds(tau));
+  int set = 0;
+  uint32_t parity = 0;
+  while (true) {
+    const TileDesc d = desc_set(set);
+    // ---- wait for the staged segments (bounded) ----
+    // Only warp 0 polls the mbarrier; the other warps wait in the block
+    // barrier, which issues nothing.  The barrier orders warp 0's acquire of
+    // the copied bytes (and its own plain stores) before every other thread's
+    // reads.
+    constexpr uint32_t kSpinLimit = 1u << 26;
+    if constexpr (COPY == 1) {
+      if (warp == 0) {
+        const bool ok = mbar_wait_bounded(bar, parity, kSpinLimit);
+        if (lane == 0) *d.status = ok ? 0 : 1;
+        if (!ok) {
+          if (lane == 0 && a.err) atomicOr(a.err, DEV_COPY_TIMEOUT);
+          mbar_wait_bounded(bar, parity, kSpinLimit);  // let copies in flight land
         }
-      } else {
-        const KeyT* xk = (cur ? k1 : k0);
-        KeyT* yk = (cur ? k0 : k1);
-        const V* xv = (cur ? v1 : v0);
-        V* yv = (cur ? v0 : v1);
-        const PlainLoad<KeyT> ld(xk);
-        const SmemArray<KeyT> yka(yk + ps + diag);
-        const SmemArray<V> xva(xv), yva(yv + ps + diag);
-        merge_window<ITEMS, KeyT, NS>(ld, cmp, ld.addr(ps), na, ld.addr(pm), nb, diag, m, lanes,
-                                      [&](int i, KeyT k, uint32_t src, bool) {
-                                    yka.put(i, k);
-                                    if constexpr (kHasVal)
-                                      yva.put(i, xva.get((int)((src - ld.base) / (uint32_t)sizeof(KeyT))));
-                                  });
       }
+    } else {
+      cp_async_wait_all();
+      if (tid == 0) *d.status = 0;
     }
     __syncthreads();
-    cur ^= 1;
-  }
-  // ---- coalesced store (+ block sample for the next round) ----
-  const KeyT* fk = (cur ? k1 : k0);
-  const V* fv = (cur ? v1 : v0);
-  for (int q = tid; q < cnt; q += NT) {
-    a.out[out_base + q] = maybe_dec<Codec>(fk[q], a.dec_on_store);
-    if constexpr (kHasVal) a.vout[out_base + q] = fv[q];
-  }
-  if (a.sample_out) {
-    const int64_t rel0 = out_base - run_base;
-    const int64_t first = (a.sample_b - rel0 % a.sample_b) % a.sample_b;
-    for (int64_t q = first + (int64_t)tid * a.sample_b; q < cnt; q += (int64_t)NT * a.sample_b) {
-      a.sample_out[run_index * a.sample_run_len + (rel0 + q) / a.sample_b] = fk[q];
+    if (*d.status) return;
+    const int cnt = (int)d.meta[3];
+    if (cnt < 0) return;  // rejected tile (never expected): nothing was copied
+    const int64_t out_base = d.meta[0];
+    const int64_t run_base = d.meta[1];
+    const int64_t run_index = d.meta[2];
+    const int* cpre = d.cpre;
+    const int* sbk = d.sbk;
+    const int* sbv = d.sbv;
+    const int64_t* gsrc = d.gsrc;
+    // a persistent CTA loads the next tile's boundary row now, so the loads
+    // complete during this tile's merge levels
+    const int64_t nxt = next_tile(tau);
+    Bounds nb_next;
+    if (PERSIST && warp == 0 && nxt < total_tiles) nb_next = load_bounds(nxt);
+
+    // ---- levels: window-aligned merges, pair by pair ----
+    // Level 0 merges staged segment pairs (2p, 2p+1) into the merge buffer;
+    // the later levels ping-pong between the merge buffer and the staging
+    // buffer, pair p of level `lev` merging the outputs of pairs 2p and 2p+1
+    // below.
+    int cur = 0;  // 0: the staging buffer holds the current input
+    for (int lev = 0, span = 2; lev == 0 || (span >> 1) < nk; ++lev, span <<= 1) {
+      const int np = (nk + span - 1) / span;
+      const int* wt = d.wst + lev * 17;
+      const unsigned lanes = __ballot_sync(0xffffffffu, tid < wt[np]);
+      if (tid < wt[np]) {
+        int p = 0;  // the last pair whose first window thread is <= tid
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1) {
+          if (p + step < np && wt[p + step] <= tid) p += step;
+        }
+        const int si = p * span;
+        const int mi = min(si + (span >> 1), nk);
+        const int ei = min(si + span, nk);
+        const int ps = cpre[si], pm = cpre[mi], pe = cpre[ei];
+        const int diag = (tid - wt[p]) * ITEMS;
+        const int m = min(ITEMS, pe - ps - diag);
+        const int na = pm - ps, nb = pe - pm;
+        if (lev == 0) {
+          // the staged keys are encoded while read only when the round's input
+          // is raw caller data (a uniform branch: two specialised loops)
+          auto level0 = [&](const auto& ld) {
+            const uint32_t A0 = ld.addr(sbk[si]);
+            const uint32_t B0 = (si + 1 < nk) ? ld.addr(sbk[si + 1]) : A0 + (uint32_t)na * sizeof(KeyT);
+            const SmemArray<KeyT> yka(k1 + ps + diag);
+            const SmemArray<V> yva(v1 + ps + diag);
+            const SmemArray<V> sva(reinterpret_cast<const V*>(stage_v));
+            const int gen = a.gen_index;
+            merge_window<ITEMS, KeyT, NS>(ld, cmp, A0, na, B0, nb, diag, m, lanes,
+                                          [&](int i, KeyT k, uint32_t src, bool ta) {
+                                            yka.put(i, k);
+                                            if constexpr (kHasVal) {
+                                              const int seg = ta ? si : si + 1;
+                                              const int off =
+                                                  (int)((src - ld.base) / (uint32_t)sizeof(KeyT)) - sbk[seg];
+                                              yva.put(i, gen ? (V)(gsrc[seg] + off) : sva.get(sbv[seg] + off));
+                                            }
+                                          });
+          };
+          if (a.enc_on_load) {
+            level0(EncLoad<KeyT, Codec>(reinterpret_cast<const KeyT*>(stage_k), 1));
+          } else {
+            level0(PlainLoad<KeyT>(reinterpret_cast<const KeyT*>(stage_k)));
+          }
+        } else {
+          const KeyT* xk = (cur ? k1 : k0);
+          KeyT* yk = (cur ? k0 : k1);
+          const V* xv = (cur ? v1 : v0);
+          V* yv = (cur ? v0 : v1);
+          const PlainLoad<KeyT> ld(xk);
+          const SmemArray<KeyT> yka(yk + ps + diag);
+          const SmemArray<V> xva(xv), yva(yv + ps + diag);
+          merge_window<ITEMS, KeyT, NS>(ld, cmp, ld.addr(ps), na, ld.addr(pm), nb, diag, m, lanes,
+                                        [&](int i, KeyT k, uint32_t src, bool) {
+                                          yka.put(i, k);
+                                          if constexpr (kHasVal)
+                                            yva.put(i, xva.get((int)((src - ld.base) / (uint32_t)sizeof(KeyT))));
+                                        });
+        }
+      }
+      __syncthreads();
+      cur ^= 1;
     }
+    // ---- coalesced store (+ block sample for the next round); in a
+    // persistent CTA whose merged tile is in the merge buffer, warp 0 stages
+    // the next tile meanwhile ----
+    const bool overlap = PERSIST && nxt < total_tiles && cur == 1;
+    if (overlap && warp == 0) stage(nxt, desc_set(set ^ 1), nb_next);
+    const int t0 = overlap ? tid - 32 : tid;
+    const int nthr = overlap ? NT - 32 : NT;
+    if (t0 >= 0) {
+      const KeyT* fk = (cur ? k1 : k0);
+      const V* fv = (cur ? v1 : v0);
+      for (int q = t0; q < cnt; q += nthr) {
+        a.out[out_base + q] = maybe_dec<Codec>(fk[q], a.dec_on_store);
+        if constexpr (kHasVal) a.vout[out_base + q] = fv[q];
+      }
+      if (a.sample_out) {
+        const int64_t rel0 = out_base - run_base;
+        const int64_t first = (a.sample_b - rel0 % a.sample_b) % a.sample_b;
+        for (int64_t q = first + (int64_t)t0 * a.sample_b; q < cnt; q += (int64_t)nthr * a.sample_b) {
+          a.sample_out[run_index * a.sample_run_len + (rel0 + q) / a.sample_b] = fk[q];
+        }
+      }
+    }
+    if (nxt >= total_tiles) return;
+    __syncthreads();  // the store has read the merged tile before it is overwritten
+    if (!overlap && warp == 0) stage(nxt, desc_set(set ^ 1), nb_next);
+    tau = nxt;
+    set ^= 1;
+    parity ^= 1;
   }
 }
 

@@ -65,7 +65,8 @@ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 struct Tune {
   int k = 32;         // fan-in per round (<= 32)
   int sample_b = 32;  // block size of the forecast sample
-  int bulk_copy = 1;  // tile staging: 1 cp.async.bulk by one warp; 2 cp.async by every warp; 0 plain loads
+  int bulk_copy = 1;  // tile staging: 1 cp.async.bulk by one warp (3: same, persistent CTAs overlapping the
+                      // next tile's staging with the store); 2 cp.async by every warp; 0 plain loads
 };
 
 // Scratch layout, computed by a dry run of the same recursion as the real run.
@@ -156,6 +157,40 @@ inline int persistent_grid(const void* kern, int threads, size_t smem, cudaError
 }
 
 // Per-kernel, per-device opt-in to large dynamic shared memory.
+// CTAs of `kern` that fit the device at once (occupancy x SMs), cached.
+inline cudaError_t resident_ctas(const void* kern, int threads, size_t smem, int* out) {
+  static std::mutex mu;
+  static const void* seen_k[64];
+  static int seen_d[64], seen_v[64];
+  static int nseen = 0;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  {
+    std::lock_guard<std::mutex> g(mu);
+    for (int i = 0; i < nseen; ++i) {
+      if (seen_k[i] == kern && seen_d[i] == dev) {
+        *out = seen_v[i];
+        return cudaSuccess;
+      }
+    }
+  }
+  int per_sm = 0, sms = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  const int v = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
+  std::lock_guard<std::mutex> g(mu);
+  if (nseen < 64) {
+    seen_k[nseen] = kern;
+    seen_d[nseen] = dev;
+    seen_v[nseen] = v;
+    ++nseen;
+  }
+  *out = v;
+  return cudaSuccess;
+}
+
 inline cudaError_t ensure_smem(const void* kern, size_t bytes) {
   static std::mutex mu;
   static const void* seen_k[256];
@@ -364,11 +399,20 @@ struct Engine {
     if (grid <= 0) return cudaSuccess;
     if (grid > 0x7fffffff) return cudaErrorInvalidConfiguration;
     using GG = Geo<VV>;
+    const bool persist = copy_mode == 3;
     auto kern = copy_mode == 2 ? merge_tiles_kernel<KeyT, VV, Cmp, Codec, GG::NT, GG::ITEMS, GG::NS, 2>
+                : persist      ? merge_tiles_kernel<KeyT, VV, Cmp, Codec, GG::NT, GG::ITEMS, GG::NS, 1, true>
                                : merge_tiles_kernel<KeyT, VV, Cmp, Codec, GG::NT, GG::ITEMS, GG::NS, 1>;
-    const size_t smem = MergeSmemLayout<KeyT, VV, GG::CAP>::bytes;
+    const size_t smem = persist ? MergeSmemLayout<KeyT, VV, GG::CAP, 2>::bytes : MergeSmemLayout<KeyT, VV, GG::CAP>::bytes;
     cudaError_t e = ensure_smem((const void*)kern, smem);
     if (e != cudaSuccess) return e;
+    if (persist) {
+      // one wave of resident CTAs; each loops over its share of the tiles
+      int slots = 0;
+      e = resident_ctas((const void*)kern, GG::NT, smem, &slots);
+      if (e != cudaSuccess) return e;
+      grid = std::min<int64_t>(grid, slots);
+    }
     const int kc = level == 0 ? KC_MERGE : KC_SAMPLE_MERGE;
     hook_before(kc, st);
     kern<<<(unsigned)grid, GG::NT, smem, st>>>(a, total_tiles);

@@ -305,12 +305,13 @@ int gms_timing_reset(void);
  *              GMS_ERR_INVALID.
  *   bulk_copy  how the merge kernel stages a tile's segments in shared
  *              memory: 1 one cp.async.bulk per segment issued by one warp
- *              (default); 2 16-byte cp.async issued by every warp; 0 a merge
- *              kernel with plain loads
+ *              (default); 3 the same with persistent CTAs that stage the
+ *              next tile while storing the current one; 2 16-byte cp.async
+ *              issued by every warp; 0 a merge kernel with plain loads
  * A tuning set here applies to every dtype and size until gms_clear_tune,
  * which returns to the autotuned table below and, for classes it does not
- * hold, the built-in defaults (k 32, sample_b 32, bulk_copy 1; bulk_copy 2
- * for 64-bit keys with a payload).
+ * hold, the built-in defaults (k 32, sample_b 32, bulk_copy 1; bulk_copy 3
+ * for sorts with a payload).
  * ------------------------------------------------------------------------- */
 int gms_set_tune(int k, int sample_b, int bulk_copy);
 int gms_get_tune(int* k, int* sample_b, int* bulk_copy);

@@ -243,10 +243,10 @@ def test_invalid_arguments(gms):
 
 # ---------------------------------------------------------------------------
 # Tuning: other fan-ins, sample block sizes and every staging mode (one bulk
-# copy per segment, 16-byte copies by every warp, plain loads) must give the
-# same bits.
+# copy per segment, the same with persistent CTAs, 16-byte copies by every
+# warp, plain loads) must give the same bits.
 TUNES = [(32, 32, 0), (2, 32, 1), (3, 16, 1), (7, 64, 1), (16, 8, 1), (32, 96, 1), (5, 100, 0), (32, 17, 1),
-         (32, 32, 2), (16, 8, 2), (3, 64, 2)]
+         (32, 32, 2), (16, 8, 2), (3, 64, 2), (32, 32, 3), (16, 8, 3), (2, 32, 3), (7, 64, 3)]
 
 
 @pytest.fixture
