@@ -14,6 +14,7 @@ torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
 DEFAULT = {"k": 32, "sample_b": 32, "bulk_copy": 1}
+DEFAULT_KV = {"k": 32, "sample_b": 32, "bulk_copy": 3}  # built-in for sorts with a payload
 
 
 @pytest.fixture
@@ -42,7 +43,7 @@ def test_autotune_i32_class(gms, oracle, clean):
     assert gms.tune_for("int32", (1 << 23) - 1) == chosen
     assert gms.tune_for("int32", 1 << 23) == DEFAULT
     assert gms.tune_for("uint32", 1 << 22) == DEFAULT
-    assert gms.tune_for("int32", 1 << 22, kv=True) == DEFAULT
+    assert gms.tune_for("int32", 1 << 22, kv=True) == DEFAULT_KV
     table = gms.autotune_table()
     assert len(table) == 1 and table[0]["log2n"] == 22 and table[0]["dtype"] == 0
     for dist in (0, 3, 6):
