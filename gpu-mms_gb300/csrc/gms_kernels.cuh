@@ -68,7 +68,8 @@ struct TileSmemLayout {
   static constexpr size_t off_v1 = off_v0 + val_bytes;
   static constexpr size_t off_pre = off_v1 + val_bytes;
   static constexpr size_t off_gs = off_pre + pre_bytes;
-  static constexpr size_t bytes = off_gs + gs_bytes;
+  static constexpr size_t off_bar = off_gs + gs_bytes;  // mbarrier of the base tile's bulk load
+  static constexpr size_t bytes = off_bar + 16;
 };
 
 __device__ __forceinline__ int64_t min64(int64_t a, int64_t b) { return a < b ? a : b; }
@@ -140,21 +141,59 @@ __global__ void __launch_bounds__(NT, (MODE == MODE_BASE && sizeof(KeyT) == 4 &&
     V rv[ITEMS];
     if constexpr (STABLE) {
       // Stable: each thread must own a contiguous chunk of the input, so the
-      // striped load is staged through shared memory.
-#pragma unroll
-      for (int i = 0; i < ITEMS; ++i) {
-        const int p = tid + i * NT;
-        if (p < cnt) {
-          sk[p] = maybe_enc<Codec>(a.in[base + p], a.enc_on_load);
-          if constexpr (kHasVal) sv[p] = a.gen_index ? (V)(base + p) : a.vin[base + p];
+      // input is staged through shared memory -- by bulk copies (TMA) for a
+      // full tile at 16-byte-aligned addresses, else by striped loads.
+      bool bulk = cnt == CAP && (reinterpret_cast<uint64_t>(a.in + base) & 15) == 0;
+      const bool copy_v = kHasVal && !a.gen_index;
+      if constexpr (kHasVal) bulk = bulk && (!copy_v || (reinterpret_cast<uint64_t>(a.vin + base) & 15) == 0);
+      if (bulk) {
+        uint64_t* bar = reinterpret_cast<uint64_t*>(smem + Lay::off_bar);
+        int* timed_out = pre;
+        if (tid == 0) {
+          const uint32_t kb = (uint32_t)(CAP * sizeof(KeyT));
+          const uint32_t vb = copy_v ? (uint32_t)(CAP * sizeof(V)) : 0u;
+          mbar_init(bar, 1);
+          fence_mbar_init();
+          mbar_arrive_expect_tx(bar, kb + vb);
+          bulk_g2s(sk, a.in + base, kb, bar);
+          if constexpr (kHasVal) {
+            if (copy_v) bulk_g2s(sv, a.vin + base, vb, bar);
+          }
         }
-      }
-      __syncthreads();
+        if (tid < 32) {
+          constexpr uint32_t kSpinLimit = 1u << 26;
+          __syncwarp();
+          const bool ok = mbar_wait_bounded(bar, 0, kSpinLimit);
+          if ((tid & 31) == 0) *timed_out = ok ? 0 : 1;
+          if (!ok) {
+            if ((tid & 31) == 0 && a.err) atomicOr(a.err, DEV_COPY_TIMEOUT);
+            mbar_wait_bounded(bar, 0, kSpinLimit);  // let the copies in flight land
+          }
+        }
+        __syncthreads();
+        if (*timed_out) return;
 #pragma unroll
-      for (int i = 0; i < ITEMS; ++i) {
-        const int p = tid * ITEMS + i;
-        r[i] = sk[p < cnt ? p : 0];
-        if constexpr (kHasVal) rv[i] = sv[p < cnt ? p : 0];
+        for (int i = 0; i < ITEMS; ++i) {
+          const int p = tid * ITEMS + i;
+          r[i] = maybe_enc<Codec>(sk[p], a.enc_on_load);
+          if constexpr (kHasVal) rv[i] = copy_v ? sv[p] : (V)(base + p);
+        }
+      } else {
+#pragma unroll
+        for (int i = 0; i < ITEMS; ++i) {
+          const int p = tid + i * NT;
+          if (p < cnt) {
+            sk[p] = maybe_enc<Codec>(a.in[base + p], a.enc_on_load);
+            if constexpr (kHasVal) sv[p] = a.gen_index ? (V)(base + p) : a.vin[base + p];
+          }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < ITEMS; ++i) {
+          const int p = tid * ITEMS + i;
+          r[i] = sk[p < cnt ? p : 0];
+          if constexpr (kHasVal) rv[i] = sv[p < cnt ? p : 0];
+        }
       }
       if (cnt < CAP) {
         KeyT m = r[0];
