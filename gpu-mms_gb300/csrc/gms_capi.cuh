@@ -23,15 +23,20 @@ namespace gms_capi {
 //               memory per SM) or 256 x 17 (64-bit keys)
 //   key/value   base and data rounds 256 x 17 (keys + payload staged: three
 //               CTAs per SM for 32-bit keys)
-//   index rounds (a block sample merged with its uint32 positions) 256 x 17
+//   index rounds (a block sample merged with its uint32 positions) 256 x 17,
+//               512 x 17 for 32-bit keys-only sorts
 constexpr int kNT = 512;
 constexpr int kItems = 17;
 using IndexGeo = gms::MergeGeo<256, 17>;
 template <class K>
 using KeysGeo = std::conditional_t<sizeof(K) == 4, gms::MergeGeo<288, 29>, gms::MergeGeo<256, 17>>;
+// keys-only 32-bit sorts: index rounds of 512 x 17, so a first-round group's
+// block sample (32 runs x 256 entries) is merged by one CTA
+template <class K>
+using KeysIndexGeo = std::conditional_t<sizeof(K) == 4, gms::MergeGeo<512, 17>, IndexGeo>;
 
 template <class K, class Codec>
-using KeysEngine = gms::Engine<K, gms::NoVal, gms::KeyLess, Codec, false, kNT, kItems, KeysGeo<K>, IndexGeo>;
+using KeysEngine = gms::Engine<K, gms::NoVal, gms::KeyLess, Codec, false, kNT, kItems, KeysGeo<K>, KeysIndexGeo<K>>;
 template <class K, class Codec>
 using KvEngine = gms::Engine<K, int32_t, gms::KeyLess, Codec, true, 256, 17, gms::MergeGeo<256, 17>, IndexGeo>;
 

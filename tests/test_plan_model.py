@@ -30,16 +30,15 @@ def test_tiles_fit_and_sort_is_stable(cap, k, b):
                 assert m <= cap
 
 
-INDEX_GEO = dict(cap=256 * 17, nt=256, items=17)  # rounds merging a block sample with its positions
-
-
-@pytest.mark.parametrize("base,nt,items", [(8192, 288, 29), (8192, 256, 17), (4352, 256, 17)])
-def test_production_geometry_one_round(base, nt, items):
+@pytest.mark.parametrize("base,nt,items,int_,iitems", [(8192, 288, 29, 512, 17), (4096, 256, 17, 256, 17),
+                                                        (4352, 256, 17, 256, 17)])
+def test_production_geometry_one_round(base, nt, items, int_, iitems):
     """The prebuilt engines' geometries: 32-bit keys-only data rounds of
-    288 x 29 (forecast tiles <= 7888 keys), 64-bit keys-only and key/value data
-    rounds of 256 x 17 (<= 4080); index rounds of 256 x 17; base tiles of 8192
-    (keys-only warp base case) or 4352 (key/value)."""
-    sample = Geometry(INDEX_GEO["cap"], 32, 32, nt=INDEX_GEO["nt"], items=INDEX_GEO["items"])
+    288 x 29 (forecast tiles <= 7888 keys) with index rounds of 512 x 17;
+    64-bit keys-only and key/value data and index rounds of 256 x 17 (<= 4080);
+    base tiles of 8192 (32-bit keys-only warp base case), 4096 (64-bit) or
+    4352 (key/value)."""
+    sample = Geometry(int_ * iitems, 32, 32, nt=int_, items=iitems)
     geo = Geometry(nt * items, 32, 32, base=base, nt=nt, items=items, sample=sample)
     rng = np.random.default_rng(0)
     for name, x in dists(rng, base * 32 + 4321):
@@ -47,7 +46,7 @@ def test_production_geometry_one_round(base, nt, items):
         assert np.array_equal(si, np.argsort(x, kind="stable")), name
         for lev, m in st.get("max_tile", []):
             assert m <= (geo if lev == 0 else sample).tile_cap
-        assert st["max_windows"] <= max(nt, INDEX_GEO["nt"])
+        assert st["max_windows"] <= max(nt, int_)
 
 
 @pytest.mark.parametrize("k,b", [(2, 2), (3, 2), (4, 4), (8, 2), (16, 2), (32, 2)])
