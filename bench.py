@@ -53,6 +53,23 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(dist, value, device="cuda"):
+    """The job's time for a per-rank duration: its maximum over all ranks
+    (replicas run concurrently, so the job ends with the slowest)."""
+    if dist is None:
+        return value
+    import torch
+
+    t = torch.tensor([float(value)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(keys_per_rank, world_size, steps, seconds):
+    """Whole-job throughput in Gkeys/s: every rank's keys over the job time."""
+    return keys_per_rank * world_size * steps / seconds / 1e9
+
+
 class ClockSampler:
     """nvidia-smi samples every 200 ms while the timed region runs."""
 
@@ -543,12 +560,9 @@ def run_ours(args):
     launches = lib.gms_launch_count() - launches0
     ms_total = e0.elapsed_time(e1)
     per_kernel = gms.timing_collect()
-    if dist:
-        t = torch.tensor([ms_total], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_total = float(t.item())
+    ms_total = max_over_ranks(dist, ms_total)
     ms_step = ms_total / args.steps
-    value = n * ws * args.steps / (ms_total * 1e-3) / 1e9
+    value = job_rate(n, ws, args.steps, ms_total * 1e-3)
 
     # ---- end to end through the C ABI with host buffers ----
     hin = torch.from_numpy(src_h).pin_memory()
@@ -564,11 +578,7 @@ def run_ours(args):
         rc = lib.gms_sort_host_i32(hin.data_ptr(), hout.data_ptr(), n, sp)
         assert rc == 0, lib.gms_last_error()
     torch.cuda.synchronize()
-    e2e_s = (time.perf_counter() - t0) / e2e_steps
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(dist, (time.perf_counter() - t0) / e2e_steps)
     e2e_ok = bool(np.array_equal(hout.numpy(), out.cpu().numpy()))
     # pipelined: the same host-to-host sorts with two in flight (the input copy
     # of step i+1 and the output copy of step i-1 overlap the sort of step i)
@@ -587,11 +597,7 @@ def run_ours(args):
             assert rc == 0, lib.gms_last_error()
         assert lib.gms_host_sync(sp) == 0
         reps.append((time.perf_counter() - t0) / e2e_steps)
-    pipe_s = sorted(reps)[1]
-    if dist:
-        t = torch.tensor([pipe_s], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        pipe_s = float(t.item())
+    pipe_s = max_over_ranks(dist, sorted(reps)[1])
     pipe_ok = all(bool(np.array_equal(h.numpy(), houts[0].numpy())) for h in houts[1:]) and e2e_ok
 
     if rank != 0:
@@ -643,10 +649,11 @@ def run_ours(args):
             "sort_frac": round(sort_bytes / (ms_step * 1e-3) / 1e9 / peak, 4),
         },
         "per_kernel_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in per_kernel.items() if v[1]},
-        "e2e": {"value": round(n * ws / e2e_s / 1e9, 3), "unit": "Gkeys/s", "h2d_bytes_per_step": n * 4,
+        "e2e": {"value": round(job_rate(n, ws, 1, e2e_s), 3), "unit": "Gkeys/s", "h2d_bytes_per_step": n * 4,
                 "d2h_bytes_per_step": n * 4, "ms_per_step": round(e2e_s * 1e3, 3),
                 "api": "gms_sort_host_i32 (synchronous, one call per step)"},
-        "e2e_pipelined": {"value": round(n * ws / pipe_s / 1e9, 3), "unit": "Gkeys/s", "h2d_bytes_per_step": n * 4,
+        "e2e_pipelined": {"value": round(job_rate(n, ws, 1, pipe_s), 3), "unit": "Gkeys/s",
+                          "h2d_bytes_per_step": n * 4,
                           "d2h_bytes_per_step": n * 4, "ms_per_step": round(pipe_s * 1e3, 3), "correct": pipe_ok,
                           "batches_ms_per_step": [round(x * 1e3, 3) for x in reps],
                           "api": "gms_sort_host_i32_async, two calls in flight, gms_host_sync at the end"},
@@ -678,7 +685,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--n", "--keys", dest="n", type=int, default=N_DEFAULT,
+                    help="keys per sort (--keys also works under torchrun, whose own options --n would prefix)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--autotune", action="store_true", help="run gms_autotune for the workload before warm-up")
     ap.add_argument("--no-extra", action="store_true", help="skip the batched and serving sections")
