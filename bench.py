@@ -265,6 +265,10 @@ def library_baselines(n, reps=5):
         return {"unavailable": f"thrust_baseline exited {r.returncode}: {r.stderr.strip()[:200]}"}
     d = json.loads(r.stdout.strip().splitlines()[-1])
     d["what"] = "thrust::sort int32 uniform: radix = keys-only (CUB radix sort), merge = user comparator (CUB merge sort)"
+    r = subprocess.run([exe, str(1 << 27), str(reps), "kv64"], capture_output=True, text=True, timeout=600)
+    if r.returncode == 0:
+        d["kv64"] = json.loads(r.stdout.strip().splitlines()[-1])
+        d["kv64"]["what"] = "thrust::stable_sort_by_key, 2^27 uint64 keys + int32 payload: radix / user comparator"
     return d
 
 
