@@ -573,16 +573,21 @@ def run_ours(args):
     hout = torch.empty_like(hin).pin_memory()
     for _ in range(3):  # untimed: the first device accesses to fresh pinned pages are slow
         assert lib.gms_sort_host_i32(hin.data_ptr(), hout.data_ptr(), n, sp) == 0
+    # three timed batches of e2e_steps calls; the median counts (the host link
+    # is shared with other tenants' jobs, so a batch can be slowed from outside)
     e2e_steps = min(args.steps, 5)
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        rc = lib.gms_sort_host_i32(hin.data_ptr(), hout.data_ptr(), n, sp)
-        assert rc == 0, lib.gms_last_error()
-    torch.cuda.synchronize()
-    e2e_s = max_over_ranks(dist, (time.perf_counter() - t0) / e2e_steps)
+    sync_reps = []
+    for _ in range(3):
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            rc = lib.gms_sort_host_i32(hin.data_ptr(), hout.data_ptr(), n, sp)
+            assert rc == 0, lib.gms_last_error()
+        torch.cuda.synchronize()
+        sync_reps.append((time.perf_counter() - t0) / e2e_steps)
+    e2e_s = max_over_ranks(dist, sorted(sync_reps)[1])
     e2e_ok = bool(np.array_equal(hout.numpy(), out.cpu().numpy()))
     # pipelined: the same host-to-host sorts with two in flight (the input copy
     # of step i+1 and the output copy of step i-1 overlap the sort of step i)
@@ -655,6 +660,7 @@ def run_ours(args):
         "per_kernel_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in per_kernel.items() if v[1]},
         "e2e": {"value": round(job_rate(n, ws, 1, e2e_s), 3), "unit": "Gkeys/s", "h2d_bytes_per_step": n * 4,
                 "d2h_bytes_per_step": n * 4, "ms_per_step": round(e2e_s * 1e3, 3),
+                "batches_ms_per_step": [round(x * 1e3, 3) for x in sync_reps],
                 "api": "gms_sort_host_i32 (synchronous, one call per step)"},
         "e2e_pipelined": {"value": round(job_rate(n, ws, 1, pipe_s), 3), "unit": "Gkeys/s",
                           "h2d_bytes_per_step": n * 4,
