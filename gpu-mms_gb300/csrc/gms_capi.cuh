@@ -19,7 +19,7 @@ namespace gms_capi {
 // keys, 2^27 uint64 / float32 keys with int32 payload):
 //   keys only   base: warp-shuffle base case (8192-key tiles for 32-bit
 //               keys, 4096 for 64-bit keys); 512 x 17 for tile_sort; data
-//               rounds 288 x 29 (32-bit keys: three CTAs of ~67 KB shared
+//               rounds 288 x 31 (32-bit keys: three CTAs of ~74 KB shared
 //               memory per SM) or 256 x 17 (64-bit keys)
 //   key/value   base and data rounds 256 x 17 (keys + payload staged: three
 //               CTAs per SM for 32-bit keys)
@@ -29,7 +29,7 @@ constexpr int kNT = 512;
 constexpr int kItems = 17;
 using IndexGeo = gms::MergeGeo<256, 17>;
 template <class K>
-using KeysGeo = std::conditional_t<sizeof(K) == 4, gms::MergeGeo<288, 29>, gms::MergeGeo<256, 17>>;
+using KeysGeo = std::conditional_t<sizeof(K) == 4, gms::MergeGeo<288, 31>, gms::MergeGeo<256, 17>>;
 // keys-only 32-bit sorts: index rounds of 512 x 17, so a first-round group's
 // block sample (32 runs x 256 entries) is merged by one CTA
 template <class K>

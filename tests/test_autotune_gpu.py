@@ -35,7 +35,7 @@ def _sort(gms, a):
 def test_autotune_i32_class(gms, oracle, clean):
     n = (1 << 22) + 12345
     got = gms.autotune("int32", n)
-    assert got["k"] in (8, 16, 32) and got["sample_b"] in (16, 32, 64) and got["bulk_copy"] in (0, 1)
+    assert got["k"] in (8, 16, 32) and got["sample_b"] in (16, 32, 64) and got["bulk_copy"] in (0, 1, 2, 3)
     assert got["ms"] > 0
     chosen = {k: got[k] for k in DEFAULT}
     # same size class (floor(log2 n) = 22) uses it; others keep the defaults

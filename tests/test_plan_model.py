@@ -30,11 +30,11 @@ def test_tiles_fit_and_sort_is_stable(cap, k, b):
                 assert m <= cap
 
 
-@pytest.mark.parametrize("base,nt,items,int_,iitems", [(8192, 288, 29, 512, 17), (4096, 256, 17, 256, 17),
+@pytest.mark.parametrize("base,nt,items,int_,iitems", [(8192, 288, 31, 512, 17), (4096, 256, 17, 256, 17),
                                                         (4352, 256, 17, 256, 17)])
 def test_production_geometry_one_round(base, nt, items, int_, iitems):
     """The prebuilt engines' geometries: 32-bit keys-only data rounds of
-    288 x 29 (forecast tiles <= 7888 keys) with index rounds of 512 x 17;
+    288 x 31 (forecast tiles <= 8432 keys) with index rounds of 512 x 17;
     64-bit keys-only and key/value data and index rounds of 256 x 17 (<= 4080);
     base tiles of 8192 (32-bit keys-only warp base case), 4096 (64-bit) or
     4352 (key/value)."""
