@@ -442,6 +442,94 @@ def serving_bench(lib, orc, seconds, rate=2000.0, lo=1 << 10, hi=1 << 26, budget
     }
 
 
+def host_trace(lib, gms, orc, n, warmup=3, trace_out=None):
+    """Timeline of one synchronous host-to-host sort (gms_sort_host_i32):
+    every kernel and every input / output copy bracketed by CUDA events on its
+    own stream.  The events add a few microseconds per launch, so the plain
+    (untraced) call time is reported beside the traced one."""
+    import numpy as np
+    import torch
+
+    src = orc.gen_i32(n, 0, SEED)
+    hin = torch.from_numpy(src).pin_memory()
+    hout = torch.empty_like(hin).pin_memory()
+    sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    for _ in range(max(warmup, 3)):  # also the first device accesses to fresh pinned pages
+        assert lib.gms_sort_host_i32(hin.data_ptr(), hout.data_ptr(), n, sp) == 0
+    plain = []
+    for _ in range(5):
+        t0 = time.perf_counter()
+        assert lib.gms_sort_host_i32(hin.data_ptr(), hout.data_ptr(), n, sp) == 0
+        plain.append(time.perf_counter() - t0)
+    gms.timing_collect()  # nothing pending from earlier calls
+    lib.gms_timing_reset()
+    lib.gms_timing_enable(1)
+    assert lib.gms_sort_host_i32(hin.data_ptr(), hout.data_ptr(), n, sp) == 0
+    lib.gms_timing_enable(0)
+    trace = gms.timing_trace()
+    per_class = gms.timing_collect()
+    h = hout.numpy()
+    # sorted, and the same multiset by sum and xor (a cheap check at full size)
+    ok = bool(np.all(h[1:] >= h[:-1]) and h.astype(np.int64).sum() == src.astype(np.int64).sum()
+              and np.bitwise_xor.reduce(h) == np.bitwise_xor.reduce(src))
+    copies = ("h2d_copy", "d2h_copy")
+    kern = [(c, a, b) for c, a, b in trace if c not in copies]
+    h2d = [(a, b) for c, a, b in trace if c == "h2d_copy"]
+    d2h = [(a, b) for c, a, b in trace if c == "d2h_copy"]
+    h2d_end = max(b for _, b in h2d)
+    d2h_start = min(a for a, _ in d2h)
+    d2h_end = max(b for _, b in d2h)
+    h2d_busy = sum(b - a for a, b in h2d)
+    d2h_busy = sum(b - a for a, b in d2h)
+    # the host link: each direction alone, and both at once on two streams
+    dev = [torch.empty_like(hin, device="cuda") for _ in range(2)]
+    side = [torch.cuda.Stream(), torch.cuda.Stream()]
+
+    def copy_ms(h2d, d2h_too, reps=3):
+        best = None
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            if h2d:
+                with torch.cuda.stream(side[0]):
+                    dev[0].copy_(hin, non_blocking=True)
+            if d2h_too:
+                with torch.cuda.stream(side[1]):
+                    hout.copy_(dev[1], non_blocking=True)
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            best = dt if best is None else min(best, dt)
+        return best
+
+    copy_ms(True, True, 1)
+    link = {"h2d_gbs": round(n * 4 / copy_ms(True, False) / 1e9, 1),
+            "d2h_gbs": round(n * 4 / copy_ms(False, True) / 1e9, 1),
+            "both_directions_gbs": round(2 * n * 4 / copy_ms(True, True) / 1e9, 1)}
+    del dev
+    if trace_out:
+        with open(trace_out, "w") as f:
+            f.write("class,start_ms,end_ms\n")
+            for c, a, b in trace:
+                f.write(f"{c},{a:.4f},{b:.4f}\n")
+    return {
+        "n": n,
+        "correct": ok,
+        "plain_ms_median": round(statistics.median(plain) * 1e3, 3),
+        "traced_ms": round(d2h_end, 3),
+        "entries": len(trace),
+        "input_landed_ms": round(h2d_end, 3),
+        "first_output_copy_ms": round(d2h_start, 3),
+        "kernels_end_ms": round(max(b for _, _, b in kern), 3),
+        "output_landed_ms": round(d2h_end, 3),
+        "h2d_gbs": round(n * 4 / (h2d_busy * 1e-3) / 1e9, 1),
+        "d2h_gbs": round(n * 4 / (d2h_busy * 1e-3) / 1e9, 1),
+        "kernel_busy_ms": round(sum(b - a for _, a, b in kern), 3),
+        "per_class_ms": {k: round(v[0], 3) for k, v in per_class.items() if v[1]},
+        "per_class_launches": {k: int(v[1]) for k, v in per_class.items() if v[1]},
+        "link": link,
+    }
+
+
 def run_reference(args):
     """CPU arm: the oracle's std::sort with every host thread."""
     import numpy as np
@@ -573,11 +661,12 @@ def run_ours(args):
     hout = torch.empty_like(hin).pin_memory()
     for _ in range(3):  # untimed: the first device accesses to fresh pinned pages are slow
         assert lib.gms_sort_host_i32(hin.data_ptr(), hout.data_ptr(), n, sp) == 0
-    # three timed batches of e2e_steps calls; the median counts (the host link
+    # five timed batches of e2e_steps calls; the median counts (the host link
     # is shared with other tenants' jobs, so a batch can be slowed from outside)
     e2e_steps = min(args.steps, 5)
+    e2e_batches = 5
     sync_reps = []
-    for _ in range(3):
+    for _ in range(e2e_batches):
         if dist:
             dist.barrier()
         torch.cuda.synchronize()
@@ -587,7 +676,7 @@ def run_ours(args):
             assert rc == 0, lib.gms_last_error()
         torch.cuda.synchronize()
         sync_reps.append((time.perf_counter() - t0) / e2e_steps)
-    e2e_s = max_over_ranks(dist, sorted(sync_reps)[1])
+    e2e_s = max_over_ranks(dist, statistics.median(sync_reps))
     e2e_ok = bool(np.array_equal(hout.numpy(), out.cpu().numpy()))
     # pipelined: the same host-to-host sorts with two in flight (the input copy
     # of step i+1 and the output copy of step i-1 overlap the sort of step i)
@@ -596,7 +685,7 @@ def run_ours(args):
         assert lib.gms_sort_host_i32_async(hin.data_ptr(), houts[i % 2].data_ptr(), n, sp) == 0
     assert lib.gms_host_sync(sp) == 0
     reps = []
-    for _ in range(3):  # three timed batches of e2e_steps calls; the median counts
+    for _ in range(e2e_batches):  # timed batches of e2e_steps calls; the median counts
         if dist:
             dist.barrier()
         torch.cuda.synchronize()
@@ -606,7 +695,7 @@ def run_ours(args):
             assert rc == 0, lib.gms_last_error()
         assert lib.gms_host_sync(sp) == 0
         reps.append((time.perf_counter() - t0) / e2e_steps)
-    pipe_s = max_over_ranks(dist, sorted(reps)[1])
+    pipe_s = max_over_ranks(dist, statistics.median(reps))
     pipe_ok = all(bool(np.array_equal(h.numpy(), houts[0].numpy())) for h in houts[1:]) and e2e_ok
 
     if rank != 0:
@@ -700,9 +789,11 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--autotune", action="store_true", help="run gms_autotune for the workload before warm-up")
     ap.add_argument("--no-extra", action="store_true", help="skip the batched and serving sections")
-    ap.add_argument("--mode", default="sort", choices=["sort", "batched", "serve", "profile"],
+    ap.add_argument("--mode", default="sort", choices=["sort", "batched", "serve", "profile", "trace"],
                     help="sort: the headline line; batched / serve: the full-size config 4 / config 5 runs; "
-                         "profile: warm-up sorts plus one sort of --n keys and nothing else (for ncu)")
+                         "profile: warm-up sorts plus one sort of --n keys and nothing else (for ncu); "
+                         "trace: the timeline of one synchronous host-to-host sort of --n keys")
+    ap.add_argument("--trace-out", default=None, help="trace mode: also write every launch and copy as CSV here")
     ap.add_argument("--rate", type=float, default=2000.0, help="serve mode: arrivals per second (0: all at once)")
     ap.add_argument("--max-size", type=int, default=1 << 26, help="serve mode: largest request (keys)")
     ap.add_argument("--seconds", type=float, default=60.0, help="serve mode: arrival window")
@@ -731,7 +822,9 @@ def main():
             torch.cuda.synchronize()
             print(json.dumps({"mode": "profile", "n": n, "sorts": args.warmup + 1}), flush=True)
             return 0
-        if args.mode == "batched":
+        if args.mode == "trace":
+            res = host_trace(lib, gms, orc, args.n, args.warmup, args.trace_out)
+        elif args.mode == "batched":
             res = batched_bench(lib, orc, total_keys=None, nseg=args.segments)
         else:
             res = serving_bench(lib, orc, seconds=args.seconds, rate=args.rate, hi=args.max_size)

@@ -37,6 +37,7 @@ struct HostPipe {
   void* dout[2] = {nullptr, nullptr};
   size_t cap = 0;
   cudaEvent_t ready[2][kChunks];
+  int64_t start[2][kChunks + 1];  // chunk boundaries in base tiles
   cudaEvent_t part[2][kOutParts];
   cudaEvent_t sorted[2];
   cudaEvent_t drained[2];
@@ -46,6 +47,30 @@ struct HostPipe {
 
 std::mutex g_pipe_mu;
 std::vector<HostPipe*> g_pipes;
+
+// Input chunk boundaries (in base tiles) for a host-fed sort of `tiles` base
+// tiles: a unit of k^q tiles, q the most early rounds (at most passes - 1)
+// whose unit still leaves eight units of input; chunks of 1, 1, 2, 4, ...
+// units, each at most a quarter of the input, the last taking the rest.  A
+// small first chunk lets the sort start after a short copy; every interior
+// boundary on a unit lets q merge rounds run chunk by chunk.  Returns the
+// chunk count and fills start[0..count].
+int chunk_plan(int64_t tiles, int k, int passes, int64_t* start) {
+  int64_t unit = 1;
+  for (int q = 0; q < passes - 1 && unit * k * 8 <= tiles; ++q) unit *= k;
+  const int64_t units = gms::ceil_div(tiles, unit);
+  const int64_t cap = std::max<int64_t>(1, units / 4);
+  int c = 0;
+  int64_t used = 0, size = 1;
+  start[0] = 0;
+  while (used < units) {
+    const int64_t take = (c == kChunks - 1) ? units - used : std::min(size, units - used);
+    used += take;
+    start[++c] = std::min(tiles, used * unit);
+    if (c > 1) size = std::min(2 * size, cap);
+  }
+  return c;
+}
 
 // Copies out the final prefix of the output after each part of the last
 // round: records an event on the sort stream, and the output-copy stream
@@ -64,9 +89,11 @@ struct OutDrain {
     cudaEvent_t ev = d->p->part[d->slot][d->used++];
     cudaError_t e = cudaEventRecord(ev, st);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(d->p->d2h, ev, 0);
+    gms::hook_before(gms::KC_D2H, d->p->d2h);
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(d->host_out + d->done, d->dev_out + d->done, sizeof(int32_t) * (size_t)(safe - d->done),
                           cudaMemcpyDeviceToHost, d->p->d2h);
+    gms::hook_after(gms::KC_D2H, d->p->d2h);
     if (e == cudaSuccess) d->done = safe;
     d->err = e;
   }
@@ -141,23 +168,24 @@ int host_sort_enqueue(const int32_t* host_in, int32_t* host_out, int64_t n, cuda
     e = cudaStreamWaitEvent(p->h2d, p->drained[slot], 0);
     if (e != cudaSuccess) return cuda_error(e, "cudaStreamWaitEvent");
   }
-  // Up to kChunks pieces of whole base tiles; a piece holds a multiple of k
-  // tiles when it can, so the first merge round also runs piece by piece.
+  // Up to kChunks pieces of whole base tiles (chunk_plan), the first one small
+  // so that the sort starts soon after the call.
   const int64_t tiles = gms::ceil_div(n, EngI32::BASE_TILE);
-  const int64_t fan = tune_for(0, 0, n).k;
-  int64_t per = gms::ceil_div(tiles, (int64_t)kChunks);
-  if (per >= fan) per = gms::ceil_div(per, fan) * fan;
+  const gms::Tune tune = tune_for(0, 0, n);
+  int64_t* start = p->start[slot];
   gms::BaseGate gate;
-  gate.tiles_per_chunk = per;
-  gate.chunks = (int)gms::ceil_div(tiles, per);
+  gate.chunks = chunk_plan(tiles, tune.k, EngI32::passes_for(n, tune.k), start);
+  gate.start = start;
   gate.ready = p->ready[slot];
   gate.early_rounds = early_rounds;
   for (int c = 0; c < gate.chunks; ++c) {
-    const int64_t k0 = std::min(n, c * gate.tiles_per_chunk * EngI32::BASE_TILE);
-    const int64_t k1 = std::min(n, (c + 1) * gate.tiles_per_chunk * EngI32::BASE_TILE);
+    const int64_t k0 = std::min(n, start[c] * EngI32::BASE_TILE);
+    const int64_t k1 = std::min(n, start[c + 1] * EngI32::BASE_TILE);
     if (k1 > k0) {
+      gms::hook_before(gms::KC_H2D, p->h2d);
       e = cudaMemcpyAsync((int32_t*)p->din[slot] + k0, host_in + k0, sizeof(int32_t) * (size_t)(k1 - k0),
                           cudaMemcpyHostToDevice, p->h2d);
+      gms::hook_after(gms::KC_H2D, p->h2d);
       if (e != cudaSuccess) return cuda_error(e, "cudaMemcpyAsync H2D");
     }
     e = cudaEventRecord(p->ready[slot][c], p->h2d);
@@ -169,6 +197,7 @@ int host_sort_enqueue(const int32_t* host_in, int32_t* host_out, int64_t n, cuda
   OutDrain drain{p, slot, host_out, (const int32_t*)p->dout[slot], 0, cudaSuccess};
   gms::RoundSplit split;
   split.parts = kOutParts;
+  split.ramp = true;
   split.after = &OutDrain::after_part;
   split.ctx = &drain;
   status = run_sort<EngI32, uint32_t, NoVal>((uint32_t*)p->din[slot], nullptr, (uint32_t*)p->dout[slot], nullptr, n, st,
@@ -177,9 +206,12 @@ int host_sort_enqueue(const int32_t* host_in, int32_t* host_out, int64_t n, cuda
   if (drain.err != cudaSuccess) return cuda_error(drain.err, "host pipeline output");
   e = cudaEventRecord(p->sorted[slot], st);
   if (e == cudaSuccess) e = cudaStreamWaitEvent(p->d2h, p->sorted[slot], 0);
-  if (e == cudaSuccess && drain.done < n)
+  if (e == cudaSuccess && drain.done < n) {
+    gms::hook_before(gms::KC_D2H, p->d2h);
     e = cudaMemcpyAsync(host_out + drain.done, (const int32_t*)p->dout[slot] + drain.done,
                         sizeof(int32_t) * (size_t)(n - drain.done), cudaMemcpyDeviceToHost, p->d2h);
+    gms::hook_after(gms::KC_D2H, p->d2h);
+  }
   if (e == cudaSuccess) e = cudaEventRecord(p->drained[slot], p->d2h);
   if (e != cudaSuccess) return cuda_error(e, "host pipeline output");
   p->used[slot] = true;

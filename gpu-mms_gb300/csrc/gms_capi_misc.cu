@@ -1,4 +1,5 @@
 // C ABI: version, status strings, error recording, scratch cache, queries.
+#include <algorithm>
 #include <mutex>
 #include <vector>
 
@@ -108,7 +109,7 @@ void before_launch(int kc, cudaStream_t st) {
 }
 void after_launch(int kc, cudaStream_t st) {
   std::lock_guard<std::mutex> g(g_prof_mu);
-  g_launches[kc]++;
+  if (kc < gms::KC_H2D) g_launches[kc]++;  // the copy classes are not kernels
   if (!g_timing) return;
   cudaEvent_t b = pool_event();
   cudaEventRecord(b, st);
@@ -201,6 +202,29 @@ int gms_timing_collect(double* ms, long long* launches, int nclasses) {
     if (launches) launches[i] = g_timed[i];
   }
   return GMS_OK;
+}
+
+int gms_timing_trace(int* classes, double* start_ms, double* end_ms, int max_entries) {
+  clear_error();
+  std::lock_guard<std::mutex> g(g_prof_mu);
+  const int n = (int)g_pending.size();
+  if (n == 0) return 0;
+  // times relative to the first recorded start, shifted so the earliest is 0
+  std::vector<float> a(n), b(n);
+  for (int i = 0; i < n; ++i) {
+    cudaError_t e = cudaEventSynchronize(g_pending[i].b);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&a[i], g_pending[0].a, g_pending[i].a);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&b[i], g_pending[0].a, g_pending[i].b);
+    if (e != cudaSuccess) return cuda_error(e, "cudaEventElapsedTime");
+  }
+  float lo = 0.f;
+  for (int i = 0; i < n; ++i) lo = std::min(lo, a[i]);
+  for (int i = 0; i < n && i < max_entries; ++i) {
+    if (classes) classes[i] = g_pending[i].kc;
+    if (start_ms) start_ms[i] = a[i] - lo;
+    if (end_ms) end_ms[i] = b[i] - lo;
+  }
+  return n;
 }
 
 int gms_timing_reset(void) {

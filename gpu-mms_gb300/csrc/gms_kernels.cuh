@@ -1017,7 +1017,7 @@ __global__ void __launch_bounds__(256) splitter_kernel(const KeyT* __restrict__ 
         // earlier runs win ties: a key precedes the boundary if key <= v
         // (lane < kb) or key < v (lane > kb)
         const bool le = lane < kb;
-        auto precedes = [&](const KeyT& x) -> bool { return le ? !cmp(v, x) : cmp(x, v); };
+        auto precedes = [=](const KeyT& x) -> bool { return le ? !cmp(v, x) : cmp(x, v); };
         // 1. blocks whose first key precedes the boundary
         const KeyT* sr = samp + (g * (int64_t)k + lane) * sample_run_len;
         const int64_t nb = (len + sample_b - 1) / sample_b;

@@ -40,7 +40,9 @@ enum KernelClass : int {
   KC_SPLIT = 3,         // splitter_kernel
   KC_GATHER = 4,        // gather_sample_kernel
   KC_CORANK = 5,        // corank_kernel
-  KC_COUNT = 6
+  KC_H2D = 6,           // host-to-device input copy of a host-fed sort (not a kernel)
+  KC_D2H = 7,           // device-to-host output copy of a host-fed sort (not a kernel)
+  KC_COUNT = 8
 };
 
 // Optional instrumentation.  The C-ABI library installs hooks that count
@@ -225,10 +227,10 @@ inline cudaError_t ensure_smem(const void* kern, size_t bytes) {
 // Host-fed base case: before the base case sorts the tiles of chunk c it makes
 // the stream wait for ready[c] (that chunk's input copy), so copies of later
 // chunks overlap the sorting of earlier ones.  Chunk c covers base tiles
-// [c * tiles_per_chunk, (c + 1) * tiles_per_chunk).
+// [start[c], start[c + 1]); start holds chunks + 1 ascending offsets from 0.
 struct BaseGate {
   int chunks = 0;
-  int64_t tiles_per_chunk = 0;
+  const int64_t* start = nullptr;
   const cudaEvent_t* ready = nullptr;
   bool early_rounds = true;  // also run the merge rounds whose groups fit a chunk, chunk by chunk
 };
@@ -240,8 +242,11 @@ struct BaseGate {
 // tile order, and tile T starts at or after (T*G - K)*B keys (each run has at
 // most one partial sample block ahead of boundary T), so after tiles [0, T)
 // at least that prefix is final.
+// With `ramp` set the first two pieces hold about 1/32 and 1/16 of the tiles
+// and the rest is split evenly, so the first final prefix is ready early.
 struct RoundSplit {
   int parts = 0;
+  bool ramp = false;
   void (*after)(void* ctx, int64_t safe, cudaStream_t st) = nullptr;
   void* ctx = nullptr;
 };
@@ -493,15 +498,30 @@ struct Engine {
     a.tiles_last = tiles_last;
     a.groups = groups;
     if (t.bulk_copy && split && split->parts > 1 && groups == 1 && tiles_last > 1) {
-      const int64_t per = ceil_div(tiles_last, (int64_t)split->parts);
-      for (int64_t t0 = 0; t0 < tiles_last; t0 += per) {
-        const int64_t t1 = std::min(tiles_last, t0 + per);
+      int64_t ends[64];
+      int np = 0;
+      const int parts = std::min(split->parts, 64);
+      if (split->ramp && parts >= 3 && tiles_last >= 64) {
+        ends[np++] = ceil_div(tiles_last, (int64_t)32);
+        ends[np++] = ends[0] + ceil_div(tiles_last, (int64_t)16);
+        const int64_t rest = ceil_div(tiles_last - ends[1], (int64_t)(parts - 2));
+        for (int64_t t1 = ends[1] + rest; np < parts; t1 += rest) ends[np++] = std::min(tiles_last, t1);
+      } else {
+        const int64_t per = ceil_div(tiles_last, (int64_t)parts);
+        for (int64_t t1 = per; np < parts; t1 += per) ends[np++] = std::min(tiles_last, t1);
+      }
+      ends[np - 1] = tiles_last;
+      int64_t t0 = 0;
+      for (int i = 0; i < np; ++i) {
+        const int64_t t1 = ends[i];
+        if (t1 <= t0) continue;
         TileArgs<KeyT, VV> b = a;
         b.tile_base = t0;
         e = launch_merge_tiles(b, t1, st, level, t.bulk_copy, t1 - t0);
         if (e != cudaSuccess) return e;
         const int64_t safe = (t1 == tiles_last) ? n : std::max<int64_t>(0, (t1 * G - k) * (int64_t)sb);
         split->after(split->ctx, std::min(safe, n), st);
+        t0 = t1;
       }
       return cudaSuccess;
     }
@@ -559,13 +579,19 @@ struct Engine {
           // Host-fed: each chunk is sorted as far as it can be on its own --
           // the base case and every round but the last whose groups fit whole
           // inside a chunk -- as soon as its copy lands.
-          const int64_t ck = gate->tiles_per_chunk * BASE_TILE;
+          // rounds whose groups start on every interior chunk boundary
           int pc = 0;
-          for (int64_t L = BASE_TILE; gate->early_rounds && pc < P - 1 && ck % (L * t.k) == 0; L *= t.k) ++pc;
+          for (int64_t gk = t.k; gate->early_rounds && pc < P - 1; gk *= t.k) {
+            bool whole = true;
+            for (int c = 1; c < gate->chunks && whole; ++c)
+              whole = gate->start[c] >= tiles || gate->start[c] % gk == 0;
+            if (!whole) break;
+            ++pc;
+          }
           for (int c = 0; c < gate->chunks && e == cudaSuccess; ++c) {
-            const int64_t t0 = c * gate->tiles_per_chunk;
+            const int64_t t0 = gate->start[c];
             if (t0 >= tiles) break;
-            const int64_t t1 = std::min(tiles, t0 + gate->tiles_per_chunk);
+            const int64_t t1 = std::min(tiles, gate->start[c + 1]);
             e = cudaStreamWaitEvent(st, gate->ready[c], 0);
             if (e != cudaSuccess) break;
             TileArgs<KeyT, V> b = a;

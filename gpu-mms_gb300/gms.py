@@ -175,6 +175,8 @@ SIGNATURES = {
     "gms_autotune_load": (_i32, [ctypes.c_char_p]),
     "gms_timing_enable": (_i32, [_i32]),
     "gms_timing_collect": (_i32, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong), _i32]),
+    "gms_timing_trace": (_i32, [ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double),
+                                ctypes.POINTER(ctypes.c_double), _i32]),
     "gms_timing_reset": (_i32, []),
     "gms_rounds": (_i32, [_i32, _i32, _i64]),
     "gms_base_tile": (_i64, [_i32, _i32]),
@@ -309,7 +311,8 @@ def find_partitions(task, size, k, ranks, stream=None):
     return out
 
 
-KERNEL_CLASSES = ["base_tile_sort", "merge_round", "sample_merge", "splitter", "sample_gather", "corank"]
+KERNEL_CLASSES = ["base_tile_sort", "merge_round", "sample_merge", "splitter", "sample_gather", "corank",
+                  "h2d_copy", "d2h_copy"]
 
 
 def timing_collect():
@@ -320,6 +323,20 @@ def timing_collect():
     cnt = (ctypes.c_longlong * n)()
     _check(lib.gms_timing_collect(ms, cnt, n), "timing_collect")
     return {name: (ms[i], cnt[i]) for i, name in enumerate(KERNEL_CLASSES)}
+
+
+def timing_trace(max_entries=100000):
+    """Recorded launches not yet collected: [(class name, start ms, end ms)],
+    in launch order, times from the earliest start.  Call before
+    timing_collect(), which consumes them."""
+    lib = load()
+    cls = (ctypes.c_int * max_entries)()
+    t0 = (ctypes.c_double * max_entries)()
+    t1 = (ctypes.c_double * max_entries)()
+    n = lib.gms_timing_trace(cls, t0, t1, max_entries)
+    if n < 0:
+        _check(n, "timing_trace")
+    return [(KERNEL_CLASSES[cls[i]], t0[i], t1[i]) for i in range(min(n, max_entries))]
 
 
 def device_status(stream=None):

@@ -281,15 +281,24 @@ int gms_device_status(void* stream, int* status_out);
  * Instrumentation (no reference counterpart: the reference times the whole
  * call with cudaEvents in its driver, src/testMM.cu:170-186).
  * Kernel classes: 0 base-case tile sort, 1 data merge round, 2 sample merge,
- * 3 splitter, 4 sample gather, 5 co-rank.
+ * 3 splitter, 4 sample gather, 5 co-rank; and two classes that are copies,
+ * not kernels, of the host-to-host sorts: 6 input (host to device), 7 output
+ * (device to host).
  * ------------------------------------------------------------------------- */
-/* Total kernels this library has launched in the process. */
+/* Total kernels this library has launched in the process (copies excluded). */
 long long gms_launch_count(void);
-/* While on, every launch is bracketed by CUDA events on its own stream. */
+/* While on, every launch (and every copy of a host-to-host sort) is
+ * bracketed by CUDA events on its own stream. */
 int gms_timing_enable(int on);
-/* Waits for the recorded events and returns, per kernel class (up to
- * nclasses entries), the accumulated milliseconds and timed launches. */
+/* Waits for the recorded events and returns, per class (up to nclasses
+ * entries), the accumulated milliseconds and timed launches; the recorded
+ * launches are then consumed. */
 int gms_timing_collect(double* ms, long long* launches, int nclasses);
+/* The recorded launches not yet collected, in launch order: class, start and
+ * end in milliseconds from the earliest start (one device clock across
+ * streams).  Fills up to max_entries and returns how many were recorded, or
+ * a negative status.  Call before gms_timing_collect. */
+int gms_timing_trace(int* classes, double* start_ms, double* end_ms, int max_entries);
 int gms_timing_reset(void);
 
 /* ---------------------------------------------------------------------------
