@@ -22,10 +22,14 @@ int sort32(void* in, void* out, int64_t n, void* st, int dtype) {
 // ---- host-to-host sorts: copy in, sort, copy out, pipelined ----
 //
 // Per (device, stream): an input-copy stream and an output-copy stream, and
-// two slots of device buffers (input/scratch and output) used alternately, so
-// that the input copy of call i+1 and the output copy of call i-1 overlap the
-// sort of call i.  Within one call the input arrives in kChunks pieces and the
-// base case sorts each piece's tiles as soon as it lands.
+// kSlots slots of device buffers (input/scratch and output).  Asynchronous
+// calls take the slots in turn, so that the input copy of call i+1 and the
+// output copy of call i-1 overlap the sort of call i, and a slot waits only
+// for the output copy of the call kSlots back; a synchronous call drains
+// before it returns and always takes slot 0.  A slot's buffers are allocated
+// when it is first used.  Within one call the input arrives in up to kChunks
+// pieces and the base case sorts each piece's tiles as soon as it lands.
+constexpr int kSlots = 3;
 constexpr int kChunks = 8;
 constexpr int kOutParts = 8;  // parts of the last merge round
 
@@ -33,16 +37,16 @@ struct HostPipe {
   int dev = 0;
   cudaStream_t st = nullptr;
   cudaStream_t h2d = nullptr, d2h = nullptr;
-  void* din[2] = {nullptr, nullptr};
-  void* dout[2] = {nullptr, nullptr};
-  size_t cap = 0;
-  cudaEvent_t ready[2][kChunks];
-  int64_t start[2][kChunks + 1];  // chunk boundaries in base tiles
-  cudaEvent_t part[2][kOutParts];
-  cudaEvent_t sorted[2];
-  cudaEvent_t drained[2];
-  bool used[2] = {false, false};
-  uint64_t calls = 0;
+  void* din[kSlots] = {};
+  void* dout[kSlots] = {};
+  size_t cap[kSlots] = {};
+  cudaEvent_t ready[kSlots][kChunks];
+  int64_t start[kSlots][kChunks + 1];  // chunk boundaries in base tiles
+  cudaEvent_t part[kSlots][kOutParts];
+  cudaEvent_t sorted[kSlots];
+  cudaEvent_t drained[kSlots];
+  bool used[kSlots] = {};
+  uint64_t async_calls = 0;
 };
 
 std::mutex g_pipe_mu;
@@ -114,7 +118,7 @@ int pipe_for(cudaStream_t st, HostPipe** out) {
   p->st = st;
   e = cudaStreamCreateWithFlags(&p->h2d, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->d2h, cudaStreamNonBlocking);
-  for (int s = 0; s < 2 && e == cudaSuccess; ++s) {
+  for (int s = 0; s < kSlots && e == cudaSuccess; ++s) {
     for (int c = 0; c < kChunks && e == cudaSuccess; ++c) e = cudaEventCreateWithFlags(&p->ready[s][c], cudaEventDisableTiming);
     for (int c = 0; c < kOutParts && e == cudaSuccess; ++c) e = cudaEventCreateWithFlags(&p->part[s][c], cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->sorted[s], cudaEventDisableTiming);
@@ -129,10 +133,11 @@ int pipe_for(cudaStream_t st, HostPipe** out) {
   return GMS_OK;
 }
 
-// early_rounds: run the early merge rounds piece by piece as the input lands
-// (worth it when nothing else overlaps the copies; a pipeline of calls
-// already overlaps them with the neighbouring sorts).
-int host_sort_enqueue(const int32_t* host_in, int32_t* host_out, int64_t n, cudaStream_t st, bool early_rounds) {
+// sync: the caller waits for this call before the next (slot 0), and the
+// early merge rounds run piece by piece as the input lands (worth it when
+// nothing else overlaps the copies; a pipeline of calls already overlaps them
+// with the neighbouring sorts).
+int host_sort_enqueue(const int32_t* host_in, int32_t* host_out, int64_t n, cudaStream_t st, bool sync) {
   clear_error();
   if (n < 0) return set_error(GMS_ERR_INVALID, "n < 0");
   if (n == 0) return GMS_OK;
@@ -143,26 +148,21 @@ int host_sort_enqueue(const int32_t* host_in, int32_t* host_out, int64_t n, cuda
   if (status != GMS_OK) return status;
   const size_t bytes = sizeof(int32_t) * (size_t)n;
   cudaError_t e = cudaSuccess;
-  if (bytes > p->cap) {
-    // growing: wait for every call in flight on this pipeline, then reallocate
-    e = cudaStreamSynchronize(p->h2d);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(p->d2h);
+  const int slot = sync ? 0 : (int)(p->async_calls++ % kSlots);
+  if (bytes > p->cap[slot]) {
+    // growing: wait for the slot's last call (its output copy ends it), then
+    // reallocate the slot
+    if (p->used[slot]) e = cudaEventSynchronize(p->drained[slot]);
     if (e != cudaSuccess) return cuda_error(e, "host pipeline drain");
-    for (int s = 0; s < 2; ++s) {
-      cudaFree(p->din[s]);
-      cudaFree(p->dout[s]);
-      p->din[s] = p->dout[s] = nullptr;
-    }
-    p->cap = 0;
-    for (int s = 0; s < 2 && e == cudaSuccess; ++s) {
-      e = cudaMalloc(&p->din[s], bytes);
-      if (e == cudaSuccess) e = cudaMalloc(&p->dout[s], bytes);
-    }
+    cudaFree(p->din[slot]);
+    cudaFree(p->dout[slot]);
+    p->din[slot] = p->dout[slot] = nullptr;
+    p->cap[slot] = 0;
+    e = cudaMalloc(&p->din[slot], bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&p->dout[slot], bytes);
     if (e != cudaSuccess) return cuda_error(e, "host pipeline buffers");
-    p->cap = bytes;
+    p->cap[slot] = bytes;
   }
-  const int slot = (int)(p->calls++ & 1);
   // the slot's previous call must have drained its output before reuse
   if (p->used[slot]) {
     e = cudaStreamWaitEvent(p->h2d, p->drained[slot], 0);
@@ -177,7 +177,7 @@ int host_sort_enqueue(const int32_t* host_in, int32_t* host_out, int64_t n, cuda
   gate.chunks = chunk_plan(tiles, tune.k, EngI32::passes_for(n, tune.k), start);
   gate.start = start;
   gate.ready = p->ready[slot];
-  gate.early_rounds = early_rounds;
+  gate.early_rounds = sync;
   for (int c = 0; c < gate.chunks; ++c) {
     const int64_t k0 = std::min(n, start[c] * EngI32::BASE_TILE);
     const int64_t k1 = std::min(n, start[c + 1] * EngI32::BASE_TILE);
@@ -247,7 +247,7 @@ void gms_capi::release_host_pipes() {
     cudaSetDevice(p->dev);
     cudaStreamSynchronize(p->h2d);
     cudaStreamSynchronize(p->d2h);
-    for (int s = 0; s < 2; ++s) {
+    for (int s = 0; s < kSlots; ++s) {
       cudaFree(p->din[s]);
       cudaFree(p->dout[s]);
       for (int c = 0; c < kChunks; ++c) cudaEventDestroy(p->ready[s][c]);

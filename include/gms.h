@@ -125,12 +125,15 @@ int gms_sort_i32_noalloc(int32_t* input, int32_t* output, int64_t n, void* strea
 int gms_sort_host_i32(const int32_t* host_in, int32_t* host_out, int64_t n, void* stream);
 /* Pipelined form (no reference counterpart): enqueues the same copy-in, sort
  * (early merge rounds on the whole array: the pipeline already overlaps the
- * copies with the neighbouring sorts) and copy-out and returns at once; `host_out` holds the result, and `host_in`
- * may be reused, after gms_host_sync(stream).  Two calls can be in flight per
- * stream: the input copy of one call and the output copy of the one before it
- * overlap the sort of the other.  The input copy is not ordered after earlier
- * work on `stream`, so `host_in` must be ready when the call is made.  Use
- * pinned host memory (pageable memory makes the copies synchronous). */
+ * copies with the neighbouring sorts) and copy-out and returns at once;
+ * `host_out` holds the result, and `host_in` may be reused, after
+ * gms_host_sync(stream).  Calls on one stream take three sets of device
+ * buffers in turn, so the input copy of one call, the sort of the call before
+ * it and the output copy of the call before that proceed together; a call's
+ * input copy waits (on the device, not the host) for the output copy of the
+ * call three back.  The input copy is not ordered after earlier work on
+ * `stream`, so `host_in` must be ready when the call is made.  Use pinned
+ * host memory (pageable memory makes the copies synchronous). */
 int gms_sort_host_i32_async(const int32_t* host_in, int32_t* host_out, int64_t n, void* stream);
 int gms_host_sync(void* stream);
 int gms_sort_host_kv_u64_i32(const uint64_t* keys_in, const int32_t* vals_in, uint64_t* keys_out,

@@ -360,6 +360,26 @@ def test_host_sort_pipelined(gms, oracle):
     assert np.array_equal(ob.numpy(), oracle.sort(big))
 
 
+def test_host_sort_async_mixed_sizes(gms, oracle):
+    # asynchronous calls of growing and shrinking sizes in flight together, so
+    # each buffer set of the pipeline grows while the others are busy, with a
+    # synchronous call (which takes the first buffer set) in between
+    lib = gms.load()
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    sizes = [100_000, 3_000_017, 50_001, 2_000_000, 6_000_011, 10, 1_000_003, 4_500_000]
+    ins = [oracle.gen_i32(n, i % 6, 70 + i) for i, n in enumerate(sizes)]
+    hins = [torch.from_numpy(x).pin_memory() for x in ins]
+    houts = [torch.empty_like(h).pin_memory() for h in hins]
+    for i, (h, o) in enumerate(zip(hins, houts)):
+        if i == 4:
+            assert lib.gms_sort_host_i32(h.data_ptr(), o.data_ptr(), sizes[i], st) == 0, lib.gms_last_error()
+        else:
+            assert lib.gms_sort_host_i32_async(h.data_ptr(), o.data_ptr(), sizes[i], st) == 0, lib.gms_last_error()
+    assert lib.gms_host_sync(st) == 0
+    for x, o in zip(ins, houts):
+        assert np.array_equal(o.numpy(), oracle.sort(x)), x.size
+
+
 # Beyond 2^31 keys (64-bit sizes and offsets everywhere): at this size the
 # result is checked through size-independent properties -- sortedness, and the
 # multiset through order-independent sums -- rather than against the oracle.
