@@ -104,6 +104,14 @@ int run_sort(K* in, V* vin, K* out, V* vout, int64_t n, cudaStream_t st, int dty
     if (status != GMS_OK) return status;
   }
   const gms::WsPtrs<K> w = gms::ws_carve<K>(l, t.k, ws);
+  gms::BaseGate g2;
+  if (gate && gate->side) {
+    // a second scratch of the same layout for the odd chunks' level buffers
+    g2 = *gate;
+    g2.alt_ws = cache_get(41, bytes, st, &status);
+    if (status != GMS_OK) return status;
+    gate = &g2;
+  }
   cudaError_t e = Eng::sort(w, in, vin, out, vout, n, t, st, gate, split);
   if (e != cudaSuccess) return cuda_error(e, "sort");
   return GMS_OK;

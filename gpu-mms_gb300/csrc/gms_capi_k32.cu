@@ -30,13 +30,16 @@ int sort32(void* in, void* out, int64_t n, void* st, int dtype) {
 // when it is first used.  Within one call the input arrives in up to kChunks
 // pieces and the base case sorts each piece's tiles as soon as it lands.
 constexpr int kSlots = 3;
-constexpr int kChunks = 8;
+constexpr int kChunks = 16;
 constexpr int kOutParts = 8;  // parts of the last merge round
 
 struct HostPipe {
   int dev = 0;
   cudaStream_t st = nullptr;
   cudaStream_t h2d = nullptr, d2h = nullptr;
+  cudaStream_t side[2] = {nullptr, nullptr};  // chunk streams of a synchronous call's early rounds
+  cudaEvent_t fork = nullptr;
+  cudaEvent_t join[2] = {nullptr, nullptr};
   void* din[kSlots] = {};
   void* dout[kSlots] = {};
   size_t cap[kSlots] = {};
@@ -54,25 +57,45 @@ std::vector<HostPipe*> g_pipes;
 
 // Input chunk boundaries (in base tiles) for a host-fed sort of `tiles` base
 // tiles: a unit of k^q tiles, q the most early rounds (at most passes - 1)
-// whose unit still leaves eight units of input; chunks of 1, 1, 2, 4, ...
-// units, each at most a quarter of the input, the last taking the rest.  A
-// small first chunk lets the sort start after a short copy; every interior
-// boundary on a unit lets q merge rounds run chunk by chunk.  Returns the
-// chunk count and fills start[0..count].
+// whose unit still leaves eight units of input, and chunks of 1, 1, 2, 3, ...
+// units rising from the start and falling to the end (the pairs taken from
+// both ends, the rest in the middle), at most kChunks.  A small first chunk
+// lets the sort start after a short copy, a small last one leaves little to
+// sort after the last copy, and every interior boundary on a unit lets q
+// merge rounds run chunk by chunk.  Returns the chunk count and fills
+// start[0..count].
 int chunk_plan(int64_t tiles, int k, int passes, int64_t* start) {
   int64_t unit = 1;
   for (int q = 0; q < passes - 1 && unit * k * 8 <= tiles; ++q) unit *= k;
   const int64_t units = gms::ceil_div(tiles, unit);
-  const int64_t cap = std::max<int64_t>(1, units / 4);
-  int c = 0;
-  int64_t used = 0, size = 1;
-  start[0] = 0;
-  while (used < units) {
-    const int64_t take = (c == kChunks - 1) ? units - used : std::min(size, units - used);
-    used += take;
-    start[++c] = std::min(tiles, used * unit);
-    if (c > 1) size = std::min(2 * size, cap);
+  int64_t front[kChunks], back[kChunks];
+  int nf = 0, nb = 0;
+  int64_t rem = units;
+  for (int i = 0; rem > 0 && nf + nb + 3 <= kChunks; ++i) {
+    const int64_t sz = i < 2 ? 1 : i;
+    if (rem < 2 * sz) break;
+    front[nf++] = sz;
+    back[nb++] = sz;
+    rem -= 2 * sz;
   }
+  // the middle: what is left, in one chunk or two
+  int64_t mid[2] = {rem, 0};
+  int nm = rem > 0 ? 1 : 0;
+  if (rem > 1 && nf + nb + 2 <= kChunks && nf > 0 && rem > 2 * front[nf - 1]) {
+    mid[0] = rem / 2;
+    mid[1] = rem - rem / 2;
+    nm = 2;
+  }
+  int c = 0;
+  int64_t used = 0;
+  start[0] = 0;
+  auto push = [&](int64_t u) {
+    used += u;
+    start[++c] = std::min(tiles, used * unit);
+  };
+  for (int i = 0; i < nf; ++i) push(front[i]);
+  for (int i = 0; i < nm; ++i) push(mid[i]);
+  for (int i = nb - 1; i >= 0; --i) push(back[i]);
   return c;
 }
 
@@ -118,6 +141,11 @@ int pipe_for(cudaStream_t st, HostPipe** out) {
   p->st = st;
   e = cudaStreamCreateWithFlags(&p->h2d, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->d2h, cudaStreamNonBlocking);
+  for (int j = 0; j < 2 && e == cudaSuccess; ++j) {
+    e = cudaStreamCreateWithFlags(&p->side[j], cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->join[j], cudaEventDisableTiming);
+  }
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming);
   for (int s = 0; s < kSlots && e == cudaSuccess; ++s) {
     for (int c = 0; c < kChunks && e == cudaSuccess; ++c) e = cudaEventCreateWithFlags(&p->ready[s][c], cudaEventDisableTiming);
     for (int c = 0; c < kOutParts && e == cudaSuccess; ++c) e = cudaEventCreateWithFlags(&p->part[s][c], cudaEventDisableTiming);
@@ -178,6 +206,13 @@ int host_sort_enqueue(const int32_t* host_in, int32_t* host_out, int64_t n, cuda
   gate.start = start;
   gate.ready = p->ready[slot];
   gate.early_rounds = sync;
+  if (sync) {
+    // chunks alternate between two streams so that one chunk's small sample
+    // merges and splitters overlap the next chunk's base case and merges
+    gate.side = p->side;
+    gate.fork = p->fork;
+    gate.join = p->join;
+  }
   for (int c = 0; c < gate.chunks; ++c) {
     const int64_t k0 = std::min(n, start[c] * EngI32::BASE_TILE);
     const int64_t k1 = std::min(n, start[c + 1] * EngI32::BASE_TILE);
@@ -255,6 +290,12 @@ void gms_capi::release_host_pipes() {
       cudaEventDestroy(p->sorted[s]);
       cudaEventDestroy(p->drained[s]);
     }
+    for (int j = 0; j < 2; ++j) {
+      cudaStreamSynchronize(p->side[j]);
+      cudaStreamDestroy(p->side[j]);
+      cudaEventDestroy(p->join[j]);
+    }
+    cudaEventDestroy(p->fork);
     cudaStreamDestroy(p->h2d);
     cudaStreamDestroy(p->d2h);
     cudaSetDevice(cur);

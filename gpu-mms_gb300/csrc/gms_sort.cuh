@@ -228,11 +228,24 @@ inline cudaError_t ensure_smem(const void* kern, size_t bytes) {
 // the stream wait for ready[c] (that chunk's input copy), so copies of later
 // chunks overlap the sorting of earlier ones.  Chunk c covers base tiles
 // [start[c], start[c + 1]); start holds chunks + 1 ascending offsets from 0.
+//
+// With `side` set (two streams) and `alt_ws` (a second scratch of the same
+// layout), chunk c runs on side[c % 2] with the level buffers of its own
+// scratch (the first for even chunks, alt_ws for odd ones; the data-level
+// samples and the status word are shared, each chunk writing its own part),
+// so the small sample merges and splitters of one chunk overlap the base case
+// and merges of the next.  The side streams start after `fork` (recorded on
+// the sort stream) and the sort stream waits for `join` on both before the
+// rounds that span chunks.
 struct BaseGate {
   int chunks = 0;
   const int64_t* start = nullptr;
   const cudaEvent_t* ready = nullptr;
   bool early_rounds = true;  // also run the merge rounds whose groups fit a chunk, chunk by chunk
+  const cudaStream_t* side = nullptr;
+  cudaEvent_t fork = nullptr;
+  const cudaEvent_t* join = nullptr;
+  void* alt_ws = nullptr;
 };
 
 // Last round in parts: the tile merge of a single-group round is launched in
@@ -588,11 +601,23 @@ struct Engine {
             if (!whole) break;
             ++pc;
           }
+          const bool two = gate->side && gate->alt_ws && gate->fork && gate->join;
+          WsPtrs<KeyT> wa = w;
+          if (two) {
+            wa = ws_carve<KeyT>(plan(n, t), t.k, gate->alt_ws);
+            wa.err = w.err;
+            wa.s1[0] = w.s1[0];
+            wa.s1[1] = w.s1[1];
+            e = cudaEventRecord(gate->fork, st);
+            for (int j = 0; j < 2 && e == cudaSuccess; ++j) e = cudaStreamWaitEvent(gate->side[j], gate->fork, 0);
+          }
           for (int c = 0; c < gate->chunks && e == cudaSuccess; ++c) {
             const int64_t t0 = gate->start[c];
             if (t0 >= tiles) break;
             const int64_t t1 = std::min(tiles, gate->start[c + 1]);
-            e = cudaStreamWaitEvent(st, gate->ready[c], 0);
+            const cudaStream_t cs = two ? gate->side[c & 1] : st;
+            const WsPtrs<KeyT>& wc = (two && (c & 1)) ? wa : w;
+            e = cudaStreamWaitEvent(cs, gate->ready[c], 0);
             if (e != cudaSuccess) break;
             TileArgs<KeyT, V> b = a;
             const int64_t off = t0 * BASE_TILE;
@@ -601,18 +626,25 @@ struct Engine {
             b.out = a.out + off;
             b.n = nc;
             b.sample_out = a.sample_out ? a.sample_out + t0 * a.sample_run_len : nullptr;
-            e = launch_base_warp(b, t1 - t0, st);
+            e = launch_base_warp(b, t1 - t0, cs);
             int cc = 0, sb = 0;
             int64_t L = BASE_TILE;
             for (int p = 0; p < pc && e == cudaSuccess; ++p) {
               const int64_t lk = L * t.k;
               const KeyT* sin = w.s1[sb] + (off / L) * ceil_div(L, t.sample_b);
               KeyT* sout = w.s1[sb ^ 1] + (off / lk) * ceil_div(lk, t.sample_b);
-              e = round<V>(w, 0, buf[cc] + off, vbuf[cc] ? vbuf[cc] + off : nullptr, buf[cc ^ 1] + off,
-                           vbuf[cc ^ 1] ? vbuf[cc ^ 1] + off : nullptr, nc, L, t, sin, sout, 0, 0, 0, st);
+              e = round<V>(wc, 0, buf[cc] + off, vbuf[cc] ? vbuf[cc] + off : nullptr, buf[cc ^ 1] + off,
+                           vbuf[cc ^ 1] ? vbuf[cc ^ 1] + off : nullptr, nc, L, t, sin, sout, 0, 0, 0, cs);
               cc ^= 1;
               sb ^= 1;
               L = lk;
+            }
+          }
+          if (two) {
+            for (int j = 0; j < 2; ++j) {
+              const cudaError_t ej = cudaEventRecord(gate->join[j], gate->side[j]);
+              const cudaError_t ew = ej == cudaSuccess ? cudaStreamWaitEvent(st, gate->join[j], 0) : ej;
+              if (e == cudaSuccess) e = ew;
             }
           }
           rounds_done = pc;

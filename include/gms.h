@@ -113,11 +113,11 @@ int gms_sort_i32_noalloc(int32_t* input, int32_t* output, int64_t n, void* strea
  * sort, copy the result to `host_out` (may equal host_in), and wait for the
  * stream.  Device buffers come from the library's per-stream cache (allocated
  * on first use, reused afterwards).  Pinned host memory gives full copy speed.
- * gms_sort_host_i32 copies the input in up to 8 pieces on a second stream and
- * sorts each piece as far as it can on its own (base case and early merge
- * rounds) as soon as it lands; the last merge round runs in 8 parts, and the
- * output prefix each part makes final is copied back while the next part
- * merges.
+ * gms_sort_host_i32 copies the input in up to 16 pieces (small first and
+ * last) on a second stream and sorts each piece as far as it can on its own
+ * (base case and early merge rounds), on two further streams in turn, as soon
+ * as it lands; the last merge round runs in 8 parts, and the output prefix
+ * each part makes final is copied back while the next part merges.
  *
  * Replaces: the reference's driver sequence cudaMemcpy H2D -> multimergesort
  * -> cudaMemcpy D2H, src/testMM.cu:167-195.
