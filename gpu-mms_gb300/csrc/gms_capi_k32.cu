@@ -57,46 +57,46 @@ std::vector<HostPipe*> g_pipes;
 
 // Input chunk boundaries (in base tiles) for a host-fed sort of `tiles` base
 // tiles: a unit of k^q tiles, q the most early rounds (at most passes - 1)
-// whose unit still leaves eight units of input, and chunks of 1, 1, 2, 3, ...
-// units rising from the start and falling to the end (the pairs taken from
-// both ends, the rest in the middle), at most kChunks.  A small first chunk
-// lets the sort start after a short copy, a small last one leaves little to
-// sort after the last copy, and every interior boundary on a unit lets q
-// merge rounds run chunk by chunk.  Returns the chunk count and fills
+// whose unit still leaves eight units of input; chunks rising 1, 1, 2, ...,
+// c-1 units from the start, a plateau of chunks of at least c units (c about
+// an eighth of the input, at most 5, the plateau chunks larger where the
+// chunk count would exceed kChunks), and falling c-1, ..., 1 to the end, the
+// remainder taking its place in the falling part.  A small first chunk lets
+// the sort start after a short copy, small last ones leave little to sort
+// after the last copy, and every interior boundary on a unit lets q merge
+// rounds run chunk by chunk.  Returns the chunk count and fills
 // start[0..count].
 int chunk_plan(int64_t tiles, int k, int passes, int64_t* start) {
   int64_t unit = 1;
   for (int q = 0; q < passes - 1 && unit * k * 8 <= tiles; ++q) unit *= k;
   const int64_t units = gms::ceil_div(tiles, unit);
-  int64_t front[kChunks], back[kChunks];
-  int nf = 0, nb = 0;
-  int64_t rem = units;
-  for (int i = 0; rem > 0 && nf + nb + 3 <= kChunks; ++i) {
-    const int64_t sz = i < 2 ? 1 : i;
-    if (rem < 2 * sz) break;
-    front[nf++] = sz;
-    back[nb++] = sz;
-    rem -= 2 * sz;
+  const int64_t c = std::max<int64_t>(1, std::min<int64_t>(units / 8, 5));
+  int64_t sizes[kChunks];
+  int n = 0;
+  sizes[n++] = 1;
+  for (int64_t s = 1; s < c; ++s) sizes[n++] = s;  // 1, 1, 2, ..., c-1
+  const int nfall = (int)(c - 1);                    // c-1, ..., 1
+  const int64_t rem = units - (1 + c * (c - 1));     // both ramps hold 1 + c(c-1) units
+  const int slots = kChunks - n - nfall - 1;
+  const int64_t plateau = rem > 0 ? std::max<int64_t>(c, gms::ceil_div(rem, (int64_t)slots)) : c;
+  const int64_t full = rem / plateau, r = rem - full * plateau;
+  for (int64_t i = 0; i < full; ++i) sizes[n++] = plateau;
+  bool placed = r == 0;
+  for (int64_t s = c - 1; s >= 1; --s) {
+    if (!placed && r >= s) {
+      sizes[n++] = r;
+      placed = true;
+    }
+    sizes[n++] = s;
   }
-  // the middle: what is left, in one chunk or two
-  int64_t mid[2] = {rem, 0};
-  int nm = rem > 0 ? 1 : 0;
-  if (rem > 1 && nf + nb + 2 <= kChunks && nf > 0 && rem > 2 * front[nf - 1]) {
-    mid[0] = rem / 2;
-    mid[1] = rem - rem / 2;
-    nm = 2;
-  }
-  int c = 0;
+  if (!placed) sizes[n++] = r;
   int64_t used = 0;
   start[0] = 0;
-  auto push = [&](int64_t u) {
-    used += u;
-    start[++c] = std::min(tiles, used * unit);
-  };
-  for (int i = 0; i < nf; ++i) push(front[i]);
-  for (int i = 0; i < nm; ++i) push(mid[i]);
-  for (int i = nb - 1; i >= 0; --i) push(back[i]);
-  return c;
+  for (int i = 0; i < n; ++i) {
+    used += sizes[i];
+    start[i + 1] = std::min(tiles, used * unit);
+  }
+  return n;
 }
 
 // Copies out the final prefix of the output after each part of the last
