@@ -30,7 +30,7 @@ int sort32(void* in, void* out, int64_t n, void* st, int dtype) {
 // when it is first used.  Within one call the input arrives in up to kChunks
 // pieces and the base case sorts each piece's tiles as soon as it lands.
 constexpr int kSlots = 3;
-constexpr int kChunks = 16;
+constexpr int kChunks = gms::kHostChunks;
 constexpr int kOutParts = 8;  // parts of the last merge round
 
 struct HostPipe {
@@ -54,50 +54,6 @@ struct HostPipe {
 
 std::mutex g_pipe_mu;
 std::vector<HostPipe*> g_pipes;
-
-// Input chunk boundaries (in base tiles) for a host-fed sort of `tiles` base
-// tiles: a unit of k^q tiles, q the most early rounds (at most passes - 1)
-// whose unit still leaves eight units of input; chunks rising 1, 1, 2, ...,
-// c-1 units from the start, a plateau of chunks of at least c units (c about
-// an eighth of the input, at most 5, the plateau chunks larger where the
-// chunk count would exceed kChunks), and falling c-1, ..., 1 to the end, the
-// remainder taking its place in the falling part.  A small first chunk lets
-// the sort start after a short copy, small last ones leave little to sort
-// after the last copy, and every interior boundary on a unit lets q merge
-// rounds run chunk by chunk.  Returns the chunk count and fills
-// start[0..count].
-int chunk_plan(int64_t tiles, int k, int passes, int64_t* start) {
-  int64_t unit = 1;
-  for (int q = 0; q < passes - 1 && unit * k * 8 <= tiles; ++q) unit *= k;
-  const int64_t units = gms::ceil_div(tiles, unit);
-  const int64_t c = std::max<int64_t>(1, std::min<int64_t>(units / 8, 5));
-  int64_t sizes[kChunks];
-  int n = 0;
-  sizes[n++] = 1;
-  for (int64_t s = 1; s < c; ++s) sizes[n++] = s;  // 1, 1, 2, ..., c-1
-  const int nfall = (int)(c - 1);                    // c-1, ..., 1
-  const int64_t rem = units - (1 + c * (c - 1));     // both ramps hold 1 + c(c-1) units
-  const int slots = kChunks - n - nfall - 1;
-  const int64_t plateau = rem > 0 ? std::max<int64_t>(c, gms::ceil_div(rem, (int64_t)slots)) : c;
-  const int64_t full = rem / plateau, r = rem - full * plateau;
-  for (int64_t i = 0; i < full; ++i) sizes[n++] = plateau;
-  bool placed = r == 0;
-  for (int64_t s = c - 1; s >= 1; --s) {
-    if (!placed && r >= s) {
-      sizes[n++] = r;
-      placed = true;
-    }
-    sizes[n++] = s;
-  }
-  if (!placed) sizes[n++] = r;
-  int64_t used = 0;
-  start[0] = 0;
-  for (int i = 0; i < n; ++i) {
-    used += sizes[i];
-    start[i + 1] = std::min(tiles, used * unit);
-  }
-  return n;
-}
 
 // Copies out the final prefix of the output after each part of the last
 // round: records an event on the sort stream, and the output-copy stream
@@ -196,13 +152,13 @@ int host_sort_enqueue(const int32_t* host_in, int32_t* host_out, int64_t n, cuda
     e = cudaStreamWaitEvent(p->h2d, p->drained[slot], 0);
     if (e != cudaSuccess) return cuda_error(e, "cudaStreamWaitEvent");
   }
-  // Up to kChunks pieces of whole base tiles (chunk_plan), the first one small
+  // Up to kChunks pieces of whole base tiles (host_chunk_plan), the first one small
   // so that the sort starts soon after the call.
   const int64_t tiles = gms::ceil_div(n, EngI32::BASE_TILE);
   const gms::Tune tune = tune_for(0, 0, n);
   int64_t* start = p->start[slot];
   gms::BaseGate gate;
-  gate.chunks = chunk_plan(tiles, tune.k, EngI32::passes_for(n, tune.k), start);
+  gate.chunks = gms::host_chunk_plan(tiles, tune.k, EngI32::passes_for(n, tune.k), start);
   gate.start = start;
   gate.ready = p->ready[slot];
   gate.early_rounds = sync;

@@ -26,6 +26,7 @@
 #include <mutex>
 #include <type_traits>
 
+#include "gms_host_plan.h"
 #include "gms_kernels.cuh"
 
 namespace gms {
@@ -256,7 +257,8 @@ struct BaseGate {
 // most one partial sample block ahead of boundary T), so after tiles [0, T)
 // at least that prefix is final.
 // With `ramp` set the first two pieces hold about 1/32 and 1/16 of the tiles
-// and the rest is split evenly, so the first final prefix is ready early.
+// and the rest is split evenly, so the first final prefix is ready early
+// (host_split_ends in gms_host_plan.h).
 struct RoundSplit {
   int parts = 0;
   bool ramp = false;
@@ -511,19 +513,8 @@ struct Engine {
     a.tiles_last = tiles_last;
     a.groups = groups;
     if (t.bulk_copy && split && split->parts > 1 && groups == 1 && tiles_last > 1) {
-      int64_t ends[64];
-      int np = 0;
-      const int parts = std::min(split->parts, 64);
-      if (split->ramp && parts >= 3 && tiles_last >= 64) {
-        ends[np++] = ceil_div(tiles_last, (int64_t)32);
-        ends[np++] = ends[0] + ceil_div(tiles_last, (int64_t)16);
-        const int64_t rest = ceil_div(tiles_last - ends[1], (int64_t)(parts - 2));
-        for (int64_t t1 = ends[1] + rest; np < parts; t1 += rest) ends[np++] = std::min(tiles_last, t1);
-      } else {
-        const int64_t per = ceil_div(tiles_last, (int64_t)parts);
-        for (int64_t t1 = per; np < parts; t1 += per) ends[np++] = std::min(tiles_last, t1);
-      }
-      ends[np - 1] = tiles_last;
+      int64_t ends[kMaxParts];
+      const int np = host_split_ends(tiles_last, split->parts, split->ramp, ends);
       int64_t t0 = 0;
       for (int i = 0; i < np; ++i) {
         const int64_t t1 = ends[i];
