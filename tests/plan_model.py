@@ -128,6 +128,13 @@ def model_round(keys, idx, L, geo, stats, level=0):
                         assert c == int(np.searchsorted(run, v, side=side))
                 desc[j, kk] = c
         doff = desc.sum(axis=1)
+        # a last round launched in parts copies out the output prefix before
+        # tile T once tiles [0, T) have run (RoundSplit in gms_sort.cuh; the
+        # last part copies the rest): an interior tile T starts at or after
+        # (T*G - K)*B keys of its group, since of the T*G sampled blocks ahead
+        # of boundary T all but the last of each run lie wholly ahead of it
+        for j in range(jg):
+            assert doff[j] >= max(0, (j * G - k) * B), (j, int(doff[j]), G, k, B)
         for j in range(jg):
             seg_k, seg_i = [], []
             for kk in range(k):
