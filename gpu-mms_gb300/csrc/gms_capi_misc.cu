@@ -88,7 +88,9 @@ std::vector<TimedLaunch> g_pending;
 std::vector<cudaEvent_t> g_event_pool;
 double g_ms[gms::KC_COUNT] = {0};
 long long g_timed[gms::KC_COUNT] = {0};
-cudaEvent_t g_open[gms::KC_COUNT];
+// the open event of each class, per host thread (launches from several
+// threads with timing on pair their own events)
+thread_local cudaEvent_t t_open[gms::KC_COUNT];
 
 cudaEvent_t pool_event() {
   if (!g_event_pool.empty()) {
@@ -104,16 +106,22 @@ cudaEvent_t pool_event() {
 void before_launch(int kc, cudaStream_t st) {
   std::lock_guard<std::mutex> g(g_prof_mu);
   if (!g_timing) return;
-  g_open[kc] = pool_event();
-  cudaEventRecord(g_open[kc], st);
+  t_open[kc] = pool_event();
+  cudaEventRecord(t_open[kc], st);
 }
 void after_launch(int kc, cudaStream_t st) {
   std::lock_guard<std::mutex> g(g_prof_mu);
   if (kc < gms::KC_H2D) g_launches[kc]++;  // the copy classes are not kernels
-  if (!g_timing) return;
+  cudaEvent_t a = t_open[kc];
+  t_open[kc] = nullptr;
+  if (!a) return;  // timing was off when the launch began
+  if (!g_timing) {  // and was switched off since
+    g_event_pool.push_back(a);
+    return;
+  }
   cudaEvent_t b = pool_event();
   cudaEventRecord(b, st);
-  g_pending.push_back(TimedLaunch{kc, g_open[kc], b});
+  g_pending.push_back(TimedLaunch{kc, a, b});
 }
 gms::Hooks g_hook_table{before_launch, after_launch};
 }  // namespace
