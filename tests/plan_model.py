@@ -96,37 +96,34 @@ def model_round(keys, idx, L, geo, stats, level=0):
         jg = tiles_last if g == groups - 1 else tiles_full
         desc = np.zeros((jg + 1, k), dtype=np.int64)
         lens = [max(0, min((kk + 1) * L, ng) - min(kk * L, ng)) for kk in range(k)]
-        for j in range(jg + 1):
-            for kk in range(k):
-                rs = min(kk * L, ng)
-                run = keys[gbase + rs:gbase + rs + lens[kk]]
-                if j == 0:
-                    c = 0
-                elif j == jg:
-                    c = lens[kk]
-                else:
-                    fpos = g * k * Ls + j * G
-                    assert fpos < len(fk)
-                    v = fk[fpos]
-                    sidx = int(fi[fpos])
-                    rr = sidx // Ls
-                    kb = rr - g * k
-                    ib = (sidx - rr * Ls) * B
-                    assert 0 <= kb < k
-                    if kk == kb:
-                        c = ib
-                    else:
-                        side = "right" if kk < kb else "left"
-                        # splitter_kernel: block sample first, then one block
-                        samp = S[(g * k + kk) * Ls:(g * k + kk) * Ls + ceil_div(lens[kk], B)]
-                        m = int(np.searchsorted(samp, v, side=side))
-                        if m == 0:
-                            c = 0
-                        else:
-                            a0, a1 = (m - 1) * B + 1, min(m * B, lens[kk])
-                            c = a0 + int(np.searchsorted(run[a0:a1], v, side=side))
-                        assert c == int(np.searchsorted(run, v, side=side))
-                desc[j, kk] = c
+        # interior boundaries j = 1 .. jg-1: the first key of block F[j*G]
+        js = np.arange(1, jg, dtype=np.int64)
+        fpos = g * k * Ls + js * G
+        assert len(js) == 0 or fpos[-1] < len(fk)
+        v = fk[fpos]
+        sidx = fi[fpos].astype(np.int64)
+        rr = sidx // Ls
+        kb = rr - g * k
+        ib = (sidx - rr * Ls) * B
+        assert np.all((kb >= 0) & (kb < k))
+        for kk in range(k):
+            rs = min(kk * L, ng)
+            run = keys[gbase + rs:gbase + rs + lens[kk]]
+            samp = S[(g * k + kk) * Ls:(g * k + kk) * Ls + ceil_div(lens[kk], B)]
+            # earlier runs win ties: keys <= v precede for runs before kb,
+            # keys < v for runs after it
+            right = kk < kb
+            exact = np.where(right, np.searchsorted(run, v, side="right"), np.searchsorted(run, v, side="left"))
+            # splitter_kernel: block sample first (m blocks whose first key
+            # precedes), then a search inside block m-1, which must bracket
+            # the exact count
+            m = np.where(right, np.searchsorted(samp, v, side="right"), np.searchsorted(samp, v, side="left"))
+            a0 = (m - 1) * B + 1
+            a1 = np.minimum(m * B, lens[kk])
+            assert np.all(np.where(m == 0, exact == 0, (a0 <= exact) & (exact <= a1)))
+            c = np.where(kk == kb, ib, exact)
+            desc[1:jg, kk] = c
+            desc[jg, kk] = lens[kk]
         doff = desc.sum(axis=1)
         # a last round launched in parts copies out the output prefix before
         # tile T once tiles [0, T) have run (RoundSplit in gms_sort.cuh; the
