@@ -16,7 +16,8 @@ input (1 GiB per copy, far above the 129 MB L2), so no step sees a warm cache.
               bounded sample of the same workload (oracle, CPU only)
 
 `--impl reference` times the CPU implementation (the oracle's std::sort with
-every host thread): the reference ships no CPU sort of its own.
+every host thread): the reference's only CPU sort is the O(n^2) selection sort
+its test driver checks small arrays with, not an implementation of the path.
 Multi-GPU (torchrun): every rank sorts its own replica; no collective on the
 data path ("replicas only"); value = keys of all ranks / max time over ranks.
 """
@@ -569,7 +570,8 @@ def run_reference(args):
         "config": {"workload": f"int32 N={n} uniform sort on the host CPU", "n": n, "sample": sample},
         "cpu_baseline": {"value": round(value, 4), "unit": "Gkeys/s", "cores": int(used), "kind": "port",
                          "sample": f"{sample} keys per step, std::sort (__gnu_parallel) on {int(used)} threads; "
-                                   "the reference has no CPU sort, so this is the oracle's std::sort"},
+                                   "the reference's only CPU sort is its test driver's O(n^2) selection sort, "
+                                   "so this is the oracle's std::sort"},
         "e2e": {"value": round(value, 4), "unit": "Gkeys/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
