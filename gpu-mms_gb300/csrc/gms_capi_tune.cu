@@ -268,10 +268,11 @@ int gms_set_tune(int k, int sample_b, int bulk_copy) {
   if (k < 2 || k > 32) return set_error(GMS_ERR_INVALID, "k must be in [2, 32]");
   if (!valid_tune(k, sample_b))
     return set_error(GMS_ERR_INVALID, "sample_b must be >= 8 and leave room for a tile (4080/sample_b > k)");
+  if (bulk_copy < 0 || bulk_copy > 3) return set_error(GMS_ERR_INVALID, "bulk_copy must be in [0, 3]");
   std::lock_guard<std::mutex> g(g_tune_mu);
   g_tune.k = k;
   g_tune.sample_b = sample_b;
-  g_tune.bulk_copy = bulk_copy < 0 ? 0 : (bulk_copy > 3 ? 1 : bulk_copy);
+  g_tune.bulk_copy = bulk_copy;
   g_tune_explicit = true;
   return GMS_OK;
 }

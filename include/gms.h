@@ -320,6 +320,8 @@ int gms_timing_reset(void);
  *              (default); 3 the same with persistent CTAs that stage the
  *              next tile while storing the current one; 2 16-byte cp.async
  *              issued by every warp; 0 a merge kernel with plain loads
+ * Out-of-range values (k outside [2, 32], sample_b below 8 or too large for
+ * k, bulk_copy outside [0, 3]) return GMS_ERR_INVALID and change nothing.
  * A tuning set here applies to every dtype and size until gms_clear_tune,
  * which returns to the autotuned table below and, for classes it does not
  * hold, the built-in defaults (k 32, sample_b 32, bulk_copy 1; bulk_copy 3

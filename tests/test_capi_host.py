@@ -1,0 +1,93 @@
+"""Host-side logic of the C ABI, run without a GPU: argument checks that come
+before any device work, and the process-wide tuning state (gms_set_tune /
+gms_get_tune / gms_clear_tune / gms_tune_for)."""
+import ctypes
+
+import pytest
+
+from conftest import load_gms_module
+
+GMS_OK, GMS_ERR_INVALID = 0, 1
+
+
+@pytest.fixture(scope="module")
+def lib():
+    mod = load_gms_module()
+    mod.build()
+    return mod.load()
+
+
+def get_tune(lib):
+    k, b, m = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    assert lib.gms_get_tune(ctypes.byref(k), ctypes.byref(b), ctypes.byref(m)) == GMS_OK
+    return k.value, b.value, m.value
+
+
+def tune_for(lib, dtype, kv, n):
+    k, b, m = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    assert lib.gms_tune_for(dtype, kv, n, ctypes.byref(k), ctypes.byref(b), ctypes.byref(m)) == GMS_OK
+    return k.value, b.value, m.value
+
+
+def test_tuning_state(lib):
+    try:
+        assert lib.gms_clear_tune() == GMS_OK
+        assert get_tune(lib) == (32, 32, 1)
+        # built-in defaults per class: staging mode 3 for sorts with a payload
+        assert tune_for(lib, 0, 0, 1 << 28) == (32, 32, 1)
+        assert tune_for(lib, 2, 1, 1 << 27) == (32, 32, 3)
+        assert lib.gms_set_tune(16, 64, 2) == GMS_OK
+        assert get_tune(lib) == (16, 64, 2)
+        # an explicit tuning applies to every class
+        assert tune_for(lib, 0, 0, 1 << 28) == (16, 64, 2)
+        assert tune_for(lib, 4, 1, 1 << 20) == (16, 64, 2)
+        # rejected values change nothing and say why
+        for args in [(1, 32, 1), (33, 32, 1), (32, 0, 1), (32, 7, 1), (32, 128, 1), (32, 32, -1), (32, 32, 4)]:
+            assert lib.gms_set_tune(*args) == GMS_ERR_INVALID, args
+            assert lib.gms_last_error() != b""
+            assert get_tune(lib) == (16, 64, 2)
+        assert lib.gms_set_tune(32, 32, 9) == GMS_ERR_INVALID
+        assert b"bulk_copy" in lib.gms_last_error()
+        for mode in range(4):
+            assert lib.gms_set_tune(8, 16, mode) == GMS_OK
+            assert get_tune(lib) == (8, 16, mode)
+    finally:
+        lib.gms_clear_tune()
+    assert get_tune(lib) == (32, 32, 1)
+
+
+def test_rounds_follow_the_fan_in(lib):
+    try:
+        assert lib.gms_rounds(0, 0, 1 << 28) == 3  # 8192 * 32^3 = 2^28
+        assert lib.gms_set_tune(16, 32, 1) == GMS_OK
+        assert lib.gms_rounds(0, 0, 1 << 28) == 4  # 8192 * 16^4 >= 2^28 > 8192 * 16^3
+        assert lib.gms_set_tune(2, 32, 1) == GMS_OK
+        assert lib.gms_rounds(0, 0, 1 << 28) == 15
+    finally:
+        lib.gms_clear_tune()
+
+
+def test_argument_checks_before_device_work(lib):
+    vp = ctypes.c_void_p
+    assert lib.gms_sort_ws(9, 0, None, None, None, None, 10, None, 0, None) == GMS_ERR_INVALID
+    assert b"dtype" in lib.gms_last_error()
+    assert lib.gms_sort_ws(0, 2, None, None, None, None, 10, None, 0, None) == GMS_ERR_INVALID
+    assert lib.gms_sort_ws(0, 0, None, None, None, None, 10, None, 0, None) == GMS_ERR_INVALID
+    assert b"workspace" in lib.gms_last_error()
+    assert lib.gms_sort_host_i32(None, None, 10, None) == GMS_ERR_INVALID
+    assert b"null" in lib.gms_last_error()
+    assert lib.gms_sort_host_i32(vp(16), vp(16), -1, None) == GMS_ERR_INVALID
+    assert lib.gms_sort_host_i32_async(None, None, 10, None) == GMS_ERR_INVALID
+    assert lib.gms_reserve(99, 0, 10, None) == GMS_ERR_INVALID
+    assert lib.gms_reserve(0, 0, -1, None) == GMS_ERR_INVALID
+    assert lib.gms_status_string(GMS_OK) == b"GMS_OK"
+    assert lib.gms_status_string(12345) == b"GMS_ERR_UNKNOWN"
+
+
+def test_workspace_size_grows_with_n(lib):
+    sizes = [lib.gms_workspace_bytes(0, 0, n) for n in (1 << 16, 1 << 20, 1 << 24, 1 << 28)]
+    assert sizes == sorted(sizes) and sizes[0] > 0
+    # about N/B keys of block sample per level: well under the keys themselves
+    assert sizes[-1] < (1 << 28) * 4 // 4
+    assert lib.gms_workspace_bytes(0, 0, 0) == 0
+    assert lib.gms_workspace_bytes(4, 1, 1 << 20) > lib.gms_workspace_bytes(0, 0, 1 << 20)
