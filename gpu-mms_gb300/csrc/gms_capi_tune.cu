@@ -139,12 +139,13 @@ int load_cache(const char* path) {
         !field_num(p, q, "k", &k) || !field_num(p, q, "sample_b", &sb) || !field_num(p, q, "bulk_copy", &bulk))
       return set_error(GMS_ERR_INVALID, "tune cache: entry lacks a field");
     field_num(p, q, "ms", &ms);
-    if (dt < 0 || dt > 5 || (kv != 0 && kv != 1) || cls < 0 || cls > 40 || !valid_tune((int)k, (int)sb))
+    if (dt < 0 || dt > 5 || (kv != 0 && kv != 1) || cls < 0 || cls > 40 || !valid_tune((int)k, (int)sb) ||
+        bulk < 0 || bulk > 3)
       return set_error(GMS_ERR_INVALID, "tune cache: entry out of range");
     gms::Tune t;
     t.k = (int)k;
     t.sample_b = (int)sb;
-    t.bulk_copy = bulk < 0 || bulk > 3 ? 1 : (int)bulk;
+    t.bulk_copy = (int)bulk;
     got.push_back(TuneEntry{(int)dt, (int)kv, (int)cls, t, ms});
     pos = b + 1;
   }
