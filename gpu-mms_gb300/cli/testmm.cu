@@ -2,7 +2,7 @@
 //
 // Same usage and output lines as GPU-MMS's ./testMM (src/testMM.cu:49-63,
 // 134-218), so its sweep scripts (scripts/allSizes.sh, raceConditions.sh, ...)
-// run unchanged against this build:
+// run unchanged against this library:
 //   usage   testmm <N>
 //   input   srand(0); N keys rand()%1024, two rand() draws per key
 //           (create_random_list, src/buildData.h:54-65)

@@ -25,7 +25,7 @@ typedef enum gms_status {
   GMS_ERR_INVALID = 1,   /* bad argument: null pointer, negative size, bad fan-in ... */
   GMS_ERR_CUDA = 2,      /* a CUDA call failed; gms_last_error() has the CUDA message */
   GMS_ERR_NOMEM = 3,     /* device scratch could not be allocated                      */
-  GMS_ERR_TOO_LARGE = 4, /* size beyond what this build supports                       */
+  GMS_ERR_TOO_LARGE = 4, /* size beyond what this library supports                     */
   GMS_ERR_INTERNAL = 5
 } gms_status;
 

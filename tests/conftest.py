@@ -1,6 +1,6 @@
 """Shared fixtures.  `gpu`-marked tests need a CUDA device and call the CUDA
 library only through its C ABI (gpu-mms_gb300/libgms.so); the oracle
-(oracle/liboracle.so) is the checker."""
+(oracle/liboracle.so) gives the expected results."""
 import ctypes
 import importlib.util
 import os

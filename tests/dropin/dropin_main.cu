@@ -26,7 +26,7 @@ __forceinline__ __device__ int rec_cmp(Rec a, Rec b) { return a.key < b.key; }
 
 // A packed 32-bit key + 32-bit value in the shape of the reference's
 // commented testType (cmp.hxx:59-73): the cast to and assignments from a
-// 64-bit CASTTYPE word that its warp shuffles need.  This build never shuffles
+// 64-bit CASTTYPE word that its warp shuffles need.  This library never shuffles
 // keys, but such a type must still compile and sort (by key, stably).
 struct PackedKV {
   int key;
