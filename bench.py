@@ -255,6 +255,30 @@ def config_sweep(lib, orc, peak, reps=5):
     return out
 
 
+def dropin_bench(lib, orc, n, iters=5):
+    """The reference's own call, multimergesort<int, cmp<int>> from the
+    header-only drop-in, through the testMM-compatible driver (its input:
+    srand(0), rand()%1024 per key), against gms_sort_i32 on the same keys
+    (the reference generator reproduced by the oracle)."""
+    import torch
+
+    exe = os.path.join(ROOT, "gpu-mms_gb300", "testmm")
+    if not os.path.exists(exe):
+        return {"unavailable": "testmm not built"}
+    r = subprocess.run([exe, str(n), str(iters)], capture_output=True, text=True, timeout=900)
+    lines = r.stdout.strip().splitlines()
+    if r.returncode != 0 or len(lines) < 2:
+        return {"unavailable": f"testmm exited {r.returncode}: {r.stderr.strip()[:200]}"}
+    avg, lo, hi = (float(x) for x in lines[0].split())
+    src = torch.from_numpy(orc.ref_random_list(n, 0)).cuda()
+    dst = torch.empty_like(src)
+    ms_capi = _sort_time(lib, lib.gms_sort_i32, [src], [dst], n, iters, torch.cuda.Stream())
+    return {"workload": f"testmm {n} {iters}: multimergesort<int, cmp<int>>, keys rand()%1024 (srand(0))",
+            "dropin_ms_min": round(lo, 4), "dropin_ms_avg": round(avg, 4), "sorted": lines[1] == "SORTED!",
+            "c_abi_ms": round(ms_capi, 4), "dropin_gkeys_s": round(n / lo / 1e6, 3),
+            "dropin_vs_c_abi": round(ms_capi / lo, 3)}
+
+
 def library_baselines(n, reps=5):
     """thrust::sort on the same kind of input: CUB radix sort (keys only) and
     CUB merge sort (user comparator), from the in-tree thrust_baseline program."""
@@ -439,7 +463,9 @@ def serving_bench(lib, orc, seconds, rate=2000.0, lo=1 << 10, hi=1 << 26, budget
         "p50_ms": round(p50.value, 3), "p99_ms": round(p99.value, 3),
         "served_gkeys_s": round(kps.value / 1e9, 3), "wall_s": round(wall, 3),
         "serial_plain_gkeys_s": round(keys_total / serial / 1e9, 3), "serial_plain_s": round(serial, 3),
-        "speedup_vs_serial": round(serial / max(wall, 1e-9), 2),
+        **({"speedup_vs_serial": round(serial / max(wall, 1e-9), 2)} if count is not None else
+           {"kept_up": bool(wall <= seconds * 1.05 + 0.05),
+            "offered_gkeys_s": round(keys_total / seconds / 1e9, 3)}),
     }
 
 
@@ -529,6 +555,36 @@ def host_trace(lib, gms, orc, n, warmup=3, trace_out=None):
         "per_class_launches": {k: int(v[1]) for k, v in per_class.items() if v[1]},
         "link": link,
     }
+
+
+def summarize(d):
+    """Compact per-configuration results: [Gkeys/s, fraction of the whole-sort
+    HBM roofline, bit-exact] per plain / key-value configuration, and the
+    headline figure of each other section."""
+    out = {}
+    for k, v in d.get("configs", {}).items():
+        out[k] = [v["gkeys_s"], v["sort_roofline_frac"], v["bit_exact"]]
+    dr = d.get("dropin", {})
+    if "dropin_gkeys_s" in dr:
+        out["dropin_int_2p28"] = {"gkeys_s": dr["dropin_gkeys_s"], "vs_c_abi": dr["dropin_vs_c_abi"],
+                                  "sorted": dr["sorted"]}
+    lb = d.get("library_baselines", {})
+    if "radix_gkeys_s" in lb:
+        out["cub_radix_merge_gkeys_s"] = [lb["radix_gkeys_s"], lb["merge_gkeys_s"]]
+    b = d.get("batched", {})
+    if "batched_gkeys_s" in b:
+        out["batched_2p29"] = {"gkeys_s": b["batched_gkeys_s"], "graph_gkeys_s": b["graph_gkeys_s"],
+                               "vs_plain": b["speedup_vs_plain"], "exact": b["bit_exact_vs_plain"]}
+    for k in ("serving", "serving_capacity", "serving_small", "serving_small_capacity"):
+        v = d.get(k)
+        if v:
+            e = {"p50_ms": v["p50_ms"], "p99_ms": v["p99_ms"], "gkeys_s": v["served_gkeys_s"]}
+            if "speedup_vs_serial" in v:
+                e["vs_serial"] = v["speedup_vs_serial"]
+            else:
+                e["kept_up"] = v["kept_up"]
+            out[k] = e
+    return out
 
 
 def run_reference(args):
@@ -652,6 +708,8 @@ def run_ours(args):
             dist.barrier()
     lib.gms_timing_enable(0)
     launches = lib.gms_launch_count() - launches0
+    # the last timed sort's output, bit-exact against torch.sort
+    ok_timed = bool(torch.equal(out, torch.sort(src)[0]))
     ms_total = e0.elapsed_time(e1)
     per_kernel = gms.timing_collect()
     ms_total = max_over_ranks(dist, ms_total)
@@ -742,7 +800,9 @@ def run_ours(args):
             "tuning": "autotuned before warm-up" if autotuned else "defaults",
             "parallelism": "replicas" if ws > 1 else "single",
             "l2": "each step sorts its own 1 GiB input copy (> 129 MB L2)",
-            "correct": ok and e2e_ok,
+            "correct": ok and ok_timed and e2e_ok,
+            "correct_checked": "last warm-up output, last timed output and the end-to-end output, "
+                               "bit-exact against torch.sort",
         },
         "roofline": {
             "bound": "hbm", "kernel": dom_name, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
@@ -767,17 +827,25 @@ def run_ours(args):
     }
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(orc, min(n, 1 << 26))
-        line["cpu_baseline_1thread"] = cpu_baseline(orc, min(n, 1 << 24), reps=1, threads=1)
+    details = {}
+    if not args.no_cpu:
+        details["cpu_baseline_1thread"] = cpu_baseline(orc, min(n, 1 << 24), reps=1, threads=1)
     if not args.no_extra:
         del inputs
         torch.cuda.empty_cache()
-        line["configs"] = config_sweep(lib, orc, peak)
-        line["library_baselines"] = library_baselines(n)
-        line["batched"] = batched_bench(lib, orc, total_keys=1 << 29)
-        line["serving"] = serving_bench(lib, orc, seconds=2.0)
-        line["serving_capacity"] = serving_bench(lib, orc, seconds=2.0, rate=0)
-        line["serving_small"] = serving_bench(lib, orc, seconds=1.0, rate=20000.0, hi=1 << 16)
-        line["serving_small_capacity"] = serving_bench(lib, orc, seconds=1.0, rate=0, hi=1 << 16)
+        details["configs"] = config_sweep(lib, orc, peak)
+        details["dropin"] = dropin_bench(lib, orc, n)
+        details["library_baselines"] = library_baselines(n)
+        details["batched"] = batched_bench(lib, orc, total_keys=1 << 29)
+        details["serving"] = serving_bench(lib, orc, seconds=2.0)
+        details["serving_capacity"] = serving_bench(lib, orc, seconds=2.0, rate=0)
+        details["serving_small"] = serving_bench(lib, orc, seconds=1.0, rate=20000.0, hi=1 << 16)
+        details["serving_small_capacity"] = serving_bench(lib, orc, seconds=1.0, rate=0, hi=1 << 16)
+    # every section in full on a line of its own, then the one JSON line with
+    # a compact summary at its end (a reader of the output's tail sees it)
+    if details:
+        print("details " + json.dumps(details), flush=True)
+        line["summary"] = summarize(details)
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

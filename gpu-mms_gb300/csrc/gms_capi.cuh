@@ -9,36 +9,18 @@
 #include <type_traits>
 
 #include "../../include/gms.h"
+#include "gms_engines.cuh"
 #include "gms_sort.cuh"
 
 namespace gms_capi {
 
-// Engines of the prebuilt dtypes.  Item counts per thread are odd, so the
-// thread-strided shared-memory accesses of a warp fall in distinct banks.
-// Geometries were chosen by timing on GB300 (2^28 int32 keys, 2^27 uint64
-// keys, 2^27 uint64 / float32 keys with int32 payload):
-//   keys only   base: warp-shuffle base case (8192-key tiles for 32-bit
-//               keys, 4096 for 64-bit keys); 512 x 17 for tile_sort; data
-//               rounds 288 x 31 (32-bit keys: three CTAs of ~74 KB shared
-//               memory per SM) or 256 x 17 (64-bit keys)
-//   key/value   base and data rounds 256 x 17 (keys + payload staged: three
-//               CTAs per SM for 32-bit keys)
-//   index rounds (a block sample merged with its uint32 positions) 256 x 17,
-//               512 x 17 for 32-bit keys-only sorts
-constexpr int kNT = 512;
-constexpr int kItems = 17;
-using IndexGeo = gms::MergeGeo<256, 17>;
-template <class K>
-using KeysGeo = std::conditional_t<sizeof(K) == 4, gms::MergeGeo<288, 31>, gms::MergeGeo<256, 17>>;
-// keys-only 32-bit sorts: index rounds of 512 x 17, so a first-round group's
-// block sample (32 runs x 256 entries) is merged by one CTA
-template <class K>
-using KeysIndexGeo = std::conditional_t<sizeof(K) == 4, gms::MergeGeo<512, 17>, IndexGeo>;
-
-template <class K, class Codec>
-using KeysEngine = gms::Engine<K, gms::NoVal, gms::KeyLess, Codec, false, kNT, kItems, KeysGeo<K>, KeysIndexGeo<K>>;
-template <class K, class Codec>
-using KvEngine = gms::Engine<K, int32_t, gms::KeyLess, Codec, true, 256, 17, gms::MergeGeo<256, 17>, IndexGeo>;
+using gms_engines::IndexGeo;
+using gms_engines::KeysEngine;
+using gms_engines::KeysGeo;
+using gms_engines::KeysIndexGeo;
+using gms_engines::KvEngine;
+using gms_engines::kItems;
+using gms_engines::kNT;
 
 // Smallest forecast-tile capacity of any prebuilt engine: a tuning must leave
 // room for a tile in every one (capacity / sample_b > k).
@@ -65,6 +47,8 @@ inline gms::Tune default_tune() { return current_tune(); }
 
 // Frees the host-sort pipelines (streams, events, staging buffers).
 void release_host_pipes();
+// Forgets the per-device addresses of the allocation-free sort's static array.
+void release_noalloc_symbols();
 
 // Sorts with caller-provided scratch (gms_sort_ws); defined per key width.
 int sort32_ws(int dtype, void* in, void* out, int64_t n, void* ws, size_t ws_bytes, cudaStream_t st);

@@ -167,6 +167,7 @@ const char* gms_last_error(void) { return g_last_error.c_str(); }
 
 void gms_release_workspaces(void) {
   release_host_pipes();
+  release_noalloc_symbols();
   std::lock_guard<std::mutex> g(g_mu);
   for (Slot& s : g_slots) {
     int cur = 0;

@@ -57,6 +57,13 @@ int scratch_ptr(void** out) {
 
 }  // namespace
 
+namespace gms_capi {
+void release_noalloc_symbols() {
+  std::lock_guard<std::mutex> g(g_sym_mu);
+  for (void*& p : g_sym_ptr) p = nullptr;
+}
+}  // namespace gms_capi
+
 extern "C" {
 
 int gms_sort_i32_noalloc(int32_t* input, int32_t* output, int64_t n, void* stream) {
@@ -81,6 +88,26 @@ int gms_sort_i32_noalloc(int32_t* input, int32_t* output, int64_t n, void* strea
   const gms::WsPtrs<uint32_t> w = gms::ws_carve<uint32_t>(l, t.k, ws);
   e = EngNoalloc::sort(w, (uint32_t*)input, nullptr, (uint32_t*)output, nullptr, n, t, st);
   return e == cudaSuccess ? GMS_OK : cuda_error(e, "gms_sort_i32_noalloc");
+}
+
+int gms_noalloc_status(void* stream, int* status_out) {
+  clear_error();
+  if (!status_out) return set_error(GMS_ERR_INVALID, "null status_out");
+  *status_out = 0;
+  void* ws = nullptr;
+  int status = scratch_ptr(&ws);
+  if (status != GMS_OK) return status;
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_error(e, "cudaStreamSynchronize");
+  // a synchronous copy into a host variable: no staging buffer of ours
+  int v = 0;
+  e = cudaMemcpy(&v, ws, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ws, 0, sizeof(int), st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_error(e, "noalloc status word");
+  *status_out = v;
+  return GMS_OK;
 }
 
 }  // extern "C"

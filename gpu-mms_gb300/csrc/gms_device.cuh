@@ -15,6 +15,7 @@
 
 #include <cstdint>
 #include <cstring>
+#include <type_traits>
 #include <utility>
 
 #include <cuda_runtime.h>
@@ -450,77 +451,70 @@ __device__ __forceinline__ void merge_thread(int s, const Ld& ld, Cmp cmp, const
 // na keys) and B (b0, nb keys), where 0 < m <= ITEMS and diag + m <= na + nb:
 // the window never crosses the end of its pair, so every thread of a warp runs
 // the same code.  `lanes` is the mask of the warp's lanes that make this call
-// (all of them reach it).  NS independent streams of H = ceil(ITEMS/NS) outputs keep NS
-// dependency chains in flight; stream s's merge-path search scans only the H+1
-// candidates after stream s-1's co-rank.  Outputs at or past m are computed
-// from in-bounds slack and dropped, never emitted.
-template <int ITEMS, class KeyT, int NS = 2, bool INNER = true, class Ld, class Cmp, class Emit>
+// (all of them reach it).  NS independent streams of H = ceil(ITEMS/NS)
+// outputs keep NS dependency chains in flight; stream q's merge-path search
+// scans only the H+1 candidates after stream q-1's co-rank.
+//
+// CHECK selects how the steps deal with the ends of the two runs:
+//   0  every step checks both run ends; outputs at or past m are computed
+//      from in-bounds slack and dropped, never emitted;
+//   1  as 0, unless no calling lane can reach a run end within its window
+//      and every window is full (a vote over `lanes`, so no divergence):
+//      then the steps run without end checks or emit predicates;
+//   2  never checked: in shared memory both runs are followed by at least
+//      ITEMS + 1 sentinel keys (the largest key under `cmp`), and all ITEMS
+//      outputs are emitted, the ITEMS - m past the pair's end into the gap
+//      after it.  Merging from an exact co-rank, a window emits the m
+//      smallest remaining keys and then, both runs spent, only sentinels, so
+//      the emitted values are those of the exact merge and the spill writes
+//      sentinels into the gap.  For keys-only merges whose equal keys are
+//      identical (the output is fixed by its values).
+template <int ITEMS, class KeyT, int NS = 2, int CHECK = 1, class Ld, class Cmp, class Emit>
 __device__ __forceinline__ void merge_window(const Ld& ld, Cmp cmp, uint32_t A0, int na, uint32_t B0, int nb, int diag,
                                              int m, unsigned lanes, const Emit& emit) {
   constexpr int H = (ITEMS + NS - 1) / NS;
   constexpr uint32_t S = sizeof(KeyT);
-  if constexpr (NS == 2) {
-    const int ia1 = merge_path<KeyT>(ld, A0, na, B0, nb, diag, cmp);
-    const int d2 = diag + H < na + nb ? diag + H : na + nb;
-    const int lo2 = d2 - nb > ia1 ? d2 - nb : ia1;
-    int hi2 = ia1 + H;
-    hi2 = hi2 < na ? hi2 : na;
-    hi2 = hi2 < d2 ? hi2 : d2;
-    const int ia2 = merge_path_in<KeyT>(ld, A0, B0, d2, lo2, hi2, cmp);
-    const uint32_t EA = A0 + (uint32_t)na * S, EB = B0 + (uint32_t)nb * S;
-    MergeCursor<KeyT> c1, c2;
-    c1.init(ld, A0 + (uint32_t)ia1 * S, EA, B0 + (uint32_t)(diag - ia1) * S, EB);
-    c2.init(ld, A0 + (uint32_t)ia2 * S, EA, B0 + (uint32_t)(d2 - ia2) * S, EB);
-    // INNER: when no calling lane of the warp can reach a run end within its
-    // window and every window is full, the lanes run the steps without end
-    // checks or emit predicates (a choice uniform over `lanes`, the mask of
-    // the warp's lanes that call this function, so no divergence).
-    const bool inner = m == ITEMS && na - ia1 >= H && nb - (diag - ia1) >= H && na - ia2 >= ITEMS - H &&
-                       nb - (d2 - ia2) >= ITEMS - H;
-    if (INNER && __all_sync(lanes, inner)) {
+  const uint32_t EA = A0 + (uint32_t)na * S, EB = B0 + (uint32_t)nb * S;
+  int iq[NS], dq[NS];
+  iq[0] = merge_path<KeyT>(ld, A0, na, B0, nb, diag, cmp);
+  dq[0] = diag;
 #pragma unroll
-      for (int i = 0; i < H; ++i) {
-        uint32_t src1;
-        bool ta1;
-        const KeyT o1 = c1.step_inner(ld, cmp, src1, ta1);
-        emit(i, o1, src1, ta1);
-        if (H + i < ITEMS) {
-          uint32_t src2;
-          bool ta2;
-          const KeyT o2 = c2.step_inner(ld, cmp, src2, ta2);
-          emit(H + i, o2, src2, ta2);
-        }
-      }
-    } else {
+  for (int q = 1; q < NS; ++q) {
+    const int d = diag + q * H < na + nb ? diag + q * H : na + nb;
+    const int lo = d - nb > iq[q - 1] ? d - nb : iq[q - 1];
+    int hi = iq[q - 1] + H;
+    hi = hi < na ? hi : na;
+    hi = hi < d ? hi : d;
+    iq[q] = merge_path_in<KeyT>(ld, A0, B0, d, lo, hi, cmp);
+    dq[q] = d;
+  }
+  MergeCursor<KeyT> c[NS];
 #pragma unroll
-      for (int i = 0; i < H; ++i) {
-        uint32_t src1;
-        bool ta1;
-        const KeyT o1 = c1.step(ld, cmp, src1, ta1);
-        if (i < m) emit(i, o1, src1, ta1);
-        if (H + i < ITEMS) {
-          uint32_t src2;
-          bool ta2;
-          const KeyT o2 = c2.step(ld, cmp, src2, ta2);
-          if (H + i < m) emit(H + i, o2, src2, ta2);
+  for (int q = 0; q < NS; ++q) c[q].init(ld, A0 + (uint32_t)iq[q] * S, EA, B0 + (uint32_t)(dq[q] - iq[q]) * S, EB);
+  bool unchecked = CHECK == 2;
+  if constexpr (CHECK == 1) {
+    bool inner = m == ITEMS;
+#pragma unroll
+    for (int q = 0; q < NS; ++q) {
+      const int hq = ITEMS - q * H < H ? ITEMS - q * H : H;  // outputs of stream q
+      inner = inner && na - iq[q] >= hq && nb - (dq[q] - iq[q]) >= hq;
+    }
+    unchecked = __all_sync(lanes, inner);
+  }
+  if (CHECK == 2 || unchecked) {
+#pragma unroll
+    for (int i = 0; i < H; ++i) {
+#pragma unroll
+      for (int q = 0; q < NS; ++q) {
+        if (q * H + i < ITEMS) {
+          uint32_t src;
+          bool ta;
+          const KeyT o = c[q].step_inner(ld, cmp, src, ta);
+          emit(q * H + i, o, src, ta);
         }
       }
     }
-  } else {
-    const uint32_t EA = A0 + (uint32_t)na * S, EB = B0 + (uint32_t)nb * S;
-    MergeCursor<KeyT> c[NS];
-    int ia = merge_path<KeyT>(ld, A0, na, B0, nb, diag, cmp);
-    c[0].init(ld, A0 + (uint32_t)ia * S, EA, B0 + (uint32_t)(diag - ia) * S, EB);
-#pragma unroll
-    for (int q = 1; q < NS; ++q) {
-      const int dq = diag + q * H < na + nb ? diag + q * H : na + nb;
-      const int lo = dq - nb > ia ? dq - nb : ia;
-      int hi = ia + H;
-      hi = hi < na ? hi : na;
-      hi = hi < dq ? hi : dq;
-      ia = merge_path_in<KeyT>(ld, A0, B0, dq, lo, hi, cmp);
-      c[q].init(ld, A0 + (uint32_t)ia * S, EA, B0 + (uint32_t)(dq - ia) * S, EB);
-    }
+  } else if constexpr (CHECK != 2) {
 #pragma unroll
     for (int i = 0; i < H; ++i) {
 #pragma unroll
@@ -535,6 +529,39 @@ __device__ __forceinline__ void merge_window(const Ld& ld, Cmp cmp, uint32_t A0,
     }
   }
 }
+
+// Keys-only merges under the default order of unsigned stored keys can pad
+// every run in shared memory with sentinels (the largest key) and merge
+// without end checks (merge_window CHECK 2).
+template <class KeyT, class V, class Cmp>
+struct SentinelMerge {
+  static constexpr bool value =
+      !HasVal<V>::value && std::is_same<Cmp, KeyLess>::value && std::is_unsigned<KeyT>::value;
+};
+// The sentinel of a padded merge: the largest unsigned key (other key types
+// are never padded; they get a value-initialised placeholder).
+template <class KeyT>
+__device__ __forceinline__ constexpr KeyT sentinel_key() {
+  if constexpr (std::is_unsigned<KeyT>::value) {
+    return (KeyT) ~(KeyT)0;
+  } else {
+    return KeyT{};
+  }
+}
+
+// Padding of sentinel-merged runs for windows of ITEMS outputs in NS streams
+// (all 0 when the merge checks run ends instead):
+//   read  sentinels a window can read past a run's end: a stream of
+//         H = ceil(ITEMS/NS) outputs loads the key after each one it takes;
+//   gap   keys between consecutive output pairs of a level: room for the
+//         ITEMS - 1 outputs a pair's last window spills past the pair's end,
+//         and for the next level's `read` sentinels.
+template <class KeyT, class V, class Cmp, int ITEMS, int NS>
+struct RunPad {
+  static constexpr bool on = SentinelMerge<KeyT, V, Cmp>::value;
+  static constexpr int read = on ? (ITEMS + NS - 1) / NS + 1 : 0;
+  static constexpr int gap = on ? (read > ITEMS - 1 ? read : ITEMS - 1) : 0;
+};
 
 // Largest pair index p (< npairs) whose start pre[p*span] is <= q.
 __device__ __forceinline__ int find_pair(const int* pre, int npairs, int span, int q) {

@@ -1,0 +1,62 @@
+// Engines of the prebuilt dtypes, shared by the C ABI (libgms.so) and the
+// header-only drop-in (include/multimergesort.hxx), which instantiates the
+// same keys-only engine in the caller's translation unit for built-in integer
+// keys under the default comparator.
+#pragma once
+
+#include <cstdint>
+#include <type_traits>
+
+#include "gms_sort.cuh"
+
+namespace gms_engines {
+
+// Item counts per thread are odd, so the thread-strided shared-memory
+// accesses of a warp fall in distinct banks.  Geometries were chosen by
+// timing on GB300 (2^28 int32 keys, 2^27 uint64 keys, 2^27 uint64 / float32
+// keys with int32 payload):
+//   keys only   base: warp-shuffle base case (8192-key tiles for 32-bit
+//               keys, 4096 for 64-bit keys); 512 x 17 for tile_sort; data
+//               rounds 288 x 31 with one merge stream per window (32-bit
+//               keys: three CTAs of ~76 KB shared memory per SM, runs padded
+//               with sentinels) or 256 x 17 (64-bit keys)
+//   key/value   base and data rounds 256 x 17 (keys + payload staged: three
+//               CTAs per SM for 32-bit keys)
+//   index rounds (a block sample merged with its uint32 positions) 256 x 17,
+//               512 x 17 for 32-bit keys-only sorts
+constexpr int kNT = 512;
+constexpr int kItems = 17;
+using IndexGeo = gms::MergeGeo<256, 17>;
+template <class Key>
+using KeysGeo = std::conditional_t<sizeof(Key) == 4, gms::MergeGeo<288, 31, 1>, gms::MergeGeo<256, 17>>;
+// keys-only 32-bit sorts: index rounds of 512 x 17, so a first-round group's
+// block sample (32 runs x 256 entries) is merged by one CTA
+template <class Key>
+using KeysIndexGeo = std::conditional_t<sizeof(Key) == 4, gms::MergeGeo<512, 17>, IndexGeo>;
+
+// (parameter names avoid the reference's single-letter macros of params.h,
+// which callers of the drop-in header include first)
+template <class Key, class Codec>
+using KeysEngine =
+    gms::Engine<Key, gms::NoVal, gms::KeyLess, Codec, false, kNT, kItems, KeysGeo<Key>, KeysIndexGeo<Key>>;
+template <class Key, class Codec>
+using KvEngine = gms::Engine<Key, int32_t, gms::KeyLess, Codec, true, 256, 17, gms::MergeGeo<256, 17>, IndexGeo>;
+
+// Built-in key types that sort through KeysEngine: the stored unsigned type
+// and the codec that maps the key's order onto it.  Integers only: their
+// equal keys are identical, so the keys-only (unstable) engine gives the same
+// bits as a stable sort.
+template <class T, class = void>
+struct BuiltinKey {
+  static constexpr bool value = false;
+};
+template <class T>
+struct BuiltinKey<T, std::enable_if_t<std::is_integral<T>::value && (sizeof(T) == 4 || sizeof(T) == 8)>> {
+  static constexpr bool value = true;
+  using Stored = std::conditional_t<sizeof(T) == 4, uint32_t, uint64_t>;
+  using Codec = std::conditional_t<std::is_signed<T>::value,
+                                   std::conditional_t<sizeof(T) == 4, gms::SignFlip32, gms::SignFlip64>,
+                                   gms::IdentityCodec<Stored>>;
+};
+
+}  // namespace gms_engines

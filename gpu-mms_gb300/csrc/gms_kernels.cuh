@@ -378,8 +378,9 @@ __global__ void __launch_bounds__(NT, (MODE == MODE_BASE && sizeof(KeyT) == 4 &&
 //
 // Reference counterpart: squareSort (GPU-MMS src/basecase/squareSort.hxx:62-131)
 // with its register sort (bitonicSort32) and shuffle merges (merge32..512).
-template <int NT, int KPL, int ITEMS_M>
+template <int NT, int KPL, int ITEMS_M, int PAD_ = 0>
 struct BaseWarpGeom {
+  static constexpr int PAD = PAD_;  // sentinel slots after every run in shared memory (0: none)
   static constexpr int TILE = NT * KPL;
   static constexpr int WARP_RUN = 32 * KPL;
   static constexpr int log2i(int x) { return x <= 1 ? 0 : 1 + log2i(x / 2); }
@@ -392,21 +393,26 @@ struct BaseWarpGeom {
 };
 
 // Each ping-pong buffer holds the tile plus slack for the reads past a pair's
-// end of the last window of a pair (at most ITEMS_M/2 + 2 keys).
-template <class KeyT, int NT, int KPL, int ITEMS_M>
+// end of the last window of a pair (at most ITEMS_M/2 + 2 keys), and with
+// sentinel padding a gap of PAD keys after every run.
+template <class KeyT, int NT, int KPL, int ITEMS_M, int PAD = 0>
 struct BaseWarpSmem {
-  using Geo = BaseWarpGeom<NT, KPL, ITEMS_M>;
-  static constexpr int SPAN = Geo::TILE + ITEMS_M;
+  using Geo = BaseWarpGeom<NT, KPL, ITEMS_M, PAD>;
+  static constexpr int SPAN = Geo::TILE + (Geo::TILE / Geo::WARP_RUN) * PAD + ITEMS_M;
   static constexpr size_t buf = ((sizeof(KeyT) * (SPAN + 4) + 15) / 16) * 16;
   static constexpr size_t off_bar = 2 * buf;  // mbarrier of the tile's bulk load
   static constexpr size_t bytes = off_bar + 16;
 };
 
-template <class KeyT, class Cmp, class Codec, int NT, int KPL, int ITEMS_M>
+// Runs in shared memory are padded with PAD sentinel keys (the largest key)
+// when the order allows it (RunPad), so the merge levels step without run-end
+// checks; the pad after each run is refilled at every level.
+template <class KeyT, class Cmp, class Codec, int NT, int KPL, int ITEMS_M, int NSB = 2>
 __global__ void __launch_bounds__(NT) base_warp_kernel(TileArgs<KeyT, NoVal> a) {
-  using Geo = BaseWarpGeom<NT, KPL, ITEMS_M>;
+  constexpr int PAD = RunPad<KeyT, NoVal, Cmp, ITEMS_M, NSB>::gap;
+  using Geo = BaseWarpGeom<NT, KPL, ITEMS_M, PAD>;
   constexpr int TILE = Geo::TILE;
-  constexpr size_t BUF = BaseWarpSmem<KeyT, NT, KPL, ITEMS_M>::buf;
+  constexpr size_t BUF = BaseWarpSmem<KeyT, NT, KPL, ITEMS_M, PAD>::buf;
   extern __shared__ __align__(16) unsigned char smem[];
   KeyT* const k0 = reinterpret_cast<KeyT*>(smem);
   KeyT* const k1 = reinterpret_cast<KeyT*>(smem + BUF);
@@ -425,7 +431,7 @@ __global__ void __launch_bounds__(NT) base_warp_kernel(TileArgs<KeyT, NoVal> a) 
   KeyT x[KPL];
   const bool bulk = cnt == TILE && (reinterpret_cast<uint64_t>(a.in + base) & 15) == 0;
   if (bulk) {
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + BaseWarpSmem<KeyT, NT, KPL, ITEMS_M>::off_bar);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + BaseWarpSmem<KeyT, NT, KPL, ITEMS_M, PAD>::off_bar);
     int* timed_out = reinterpret_cast<int*>(smem) + 0;  // k0[0], free until the warp runs are stored
     if (tid == 0) {
       mbar_init(bar, 1);
@@ -471,11 +477,17 @@ __global__ void __launch_bounds__(NT) base_warp_kernel(TileArgs<KeyT, NoVal> a) 
   }
   network_sort<KPL>(x, cmp);
   warp_merge_runs<KPL>(x, cmp);
-  // The warp's sorted run: lane l holds elements l*KPL .. l*KPL+KPL-1.
+  // The warp's sorted run: lane l holds elements l*KPL .. l*KPL+KPL-1.  With
+  // padding, run w starts at w*(WARP_RUN + PAD) and is followed by PAD
+  // sentinels.
   {
-    const SmemArray<KeyT> dst(k0 + warp * Geo::WARP_RUN + lane * KPL);
+    KeyT* run = k0 + warp * (Geo::WARP_RUN + PAD);
+    const SmemArray<KeyT> dst(run + lane * KPL);
 #pragma unroll
     for (int r = 0; r < KPL; ++r) dst.put(r, x[r]);
+    if constexpr (PAD > 0) {
+      for (int j = lane; j < PAD; j += 32) run[Geo::WARP_RUN + j] = sentinel_key<KeyT>();
+    }
   }
   __syncthreads();
   // shared-memory merge levels: runs of WARP_RUN ... TILE/2.  Each pair of a
@@ -485,18 +497,30 @@ __global__ void __launch_bounds__(NT) base_warp_kernel(TileArgs<KeyT, NoVal> a) 
   for (int lv = 0; lv < Geo::LEVELS; ++lv) {
     const int rl = Geo::WARP_RUN << lv;
     const int tpp = (2 * rl + ITEMS_M - 1) / ITEMS_M;
+    const int np = TILE / (2 * rl);
     const KeyT* xk = cur ? k1 : k0;
     KeyT* yk = cur ? k0 : k1;
-    const unsigned lanes = __ballot_sync(0xffffffffu, tid < tpp * (TILE / (2 * rl)));
-    if (tid < tpp * (TILE / (2 * rl))) {
+    const unsigned lanes = __ballot_sync(0xffffffffu, tid < tpp * np);
+    if (tid < tpp * np) {
       const int p = tid / tpp;
       const int diag = (tid - p * tpp) * ITEMS_M;
-      const int ps = p * 2 * rl;
       const int m = min(ITEMS_M, 2 * rl - diag);
       const PlainLoad<KeyT> ld(xk);
-      const SmemArray<KeyT> yka(yk + ps + diag);
-      merge_window<ITEMS_M, KeyT, 2, false>(ld, cmp, ld.addr(ps), rl, ld.addr(ps + rl), rl, diag, m, lanes,
-                                     [&](int i, KeyT k, uint32_t, bool) { yka.put(i, k); });
+      // input runs 2p and 2p+1 (length rl, PAD apart); output pair p
+      const SmemArray<KeyT> yka(yk + p * (2 * rl + PAD) + diag);
+      merge_window<ITEMS_M, KeyT, NSB, (PAD > 0 ? 2 : 0)>(
+          ld, cmp, ld.addr(2 * p * (rl + PAD)), rl, ld.addr((2 * p + 1) * (rl + PAD)), rl, diag, m, lanes,
+          [&](int i, KeyT k, uint32_t, bool) { yka.put(i, k); });
+    }
+    if constexpr (PAD > 0) {
+      // sentinels after every output pair, read by the next level (the
+      // windows that end a pair spill the same value into the gap)
+      if (lv + 1 < Geo::LEVELS) {
+        for (int x2 = tid; x2 < np * PAD; x2 += NT) {
+          const int p = x2 / PAD;
+          yk[p * (2 * rl + PAD) + 2 * rl + (x2 - p * PAD)] = sentinel_key<KeyT>();
+        }
+      }
     }
     __syncthreads();
     cur ^= 1;
@@ -521,15 +545,25 @@ __global__ void __launch_bounds__(NT) base_warp_kernel(TileArgs<KeyT, NoVal> a) 
 // ping-pong between the merge buffer and the (now free) staging buffer.  Three
 // CTAs of 512 threads fit an SM for 4-byte keys, so one CTA's copy latency is
 // covered by the others' merging.
-template <class KeyT, class V, int CAP, int SETS = 1>
+// With sentinel padding (RunPad: READ sentinels after each staged segment,
+// GAP keys after each output pair of a level) the buffers are sized by the
+// tile limit TMAX plus the padding instead of by CAP.
+template <class KeyT, class V, int CAP, int SETS = 1, int READ = 0, int GAP = 0, int TMAX = CAP, int ITEMS = 0>
 struct MergeSmemLayout {
   static constexpr bool kHasVal = HasVal<V>::value;
   static constexpr int kMaxK = 32;
   static constexpr size_t round16(size_t x) { return (x + 15) / 16 * 16; }
-  // every segment region may add up to 30 bytes of alignment slack
-  static constexpr size_t stage_k_bytes = round16(sizeof(KeyT) * (CAP + 4) + 32 * kMaxK + 16);
+  // every segment region may add up to 30 bytes of alignment slack; a padded
+  // segment's region holds its keys and READ sentinels from a start at most 12
+  // bytes into its first 16, rounded up to 16
+  static constexpr size_t stage_k_bytes =
+      READ ? round16(sizeof(KeyT) * TMAX + kMaxK * (sizeof(KeyT) * READ + 27) + 16)
+           : round16(sizeof(KeyT) * (CAP + 4) + 32 * kMaxK + 16);
   static constexpr size_t stage_v_bytes = kHasVal ? round16(sizeof(V) * (CAP + 4) + 32 * kMaxK + 16) : 0;
-  static constexpr size_t mk_bytes = round16(sizeof(KeyT) * (CAP + 4));
+  // the merge buffer takes the even levels' outputs: up to kMaxK/2 pairs, GAP
+  // apart, and the last window's spill of up to ITEMS - 1 keys
+  static constexpr size_t mk_bytes =
+      READ ? round16(sizeof(KeyT) * (TMAX + (kMaxK / 2) * GAP + ITEMS + 4)) : round16(sizeof(KeyT) * (CAP + 4));
   static constexpr size_t mv_bytes = kHasVal ? round16(sizeof(V) * (CAP + 4)) : 0;
   static constexpr size_t off_stage_v = stage_k_bytes;
   static constexpr size_t off_mk = off_stage_v + stage_v_bytes;
@@ -581,13 +615,26 @@ struct TileDesc {
 // PERSIST (with COPY 1): each CTA loops over tiles blockIdx.x + i*gridDim.x;
 // when the merged tile ends in the merge buffer, warp 0 stages the next tile
 // into the free staging buffer while the other warps store the current one.
+template <class KeyT, class V, class Cmp, int NT, int ITEMS, int NS, bool PERSIST>
+using MergeLayoutOf =
+    MergeSmemLayout<KeyT, V, NT * ITEMS, PERSIST ? 2 : 1, RunPad<KeyT, V, Cmp, ITEMS, NS>::read,
+                    RunPad<KeyT, V, Cmp, ITEMS, NS>::gap, WindowCap<NT, ITEMS>::value, ITEMS>;
+
+// Keys-only merges under the default order pad every run with sentinels
+// (RunPad): staged segment s is followed by READ sentinels in its region, and
+// level outputs are laid out with a gap of PAD keys after every pair (pair p
+// of a level starts at cpre[first segment] + p*PAD), refilled with sentinels
+// at every level, so the merge steps never check run ends (merge_window CHECK
+// 2).  Without padding (payload merges, user comparators) the steps check.
 template <class KeyT, class V, class Cmp, class Codec, int NT, int ITEMS, int NS, int COPY = 1, bool PERSIST = false>
 __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, int64_t total_tiles) {
   static_assert(!PERSIST || COPY == 1, "persistent tiles stage with bulk copies");
   constexpr int CAP = NT * ITEMS;                        // shared-memory buffers
   constexpr int TILE_MAX = WindowCap<NT, ITEMS>::value;  // keys a tile may hold
   constexpr bool kHasVal = HasVal<V>::value;
-  using Lay = MergeSmemLayout<KeyT, V, CAP, PERSIST ? 2 : 1>;
+  constexpr int READ = RunPad<KeyT, V, Cmp, ITEMS, NS>::read;
+  constexpr int PAD = RunPad<KeyT, V, Cmp, ITEMS, NS>::gap;
+  using Lay = MergeLayoutOf<KeyT, V, Cmp, NT, ITEMS, NS, PERSIST>;
   static_assert(Lay::off_desc % 16 == 0 && Lay::set_gsrc % 8 == 0, "descriptor alignment");
   extern __shared__ __align__(16) unsigned char smem[];
   unsigned char* stage_k = smem;
@@ -673,7 +720,12 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
     const uint64_t A = arr_k_lo + (uint64_t)gs * sizeof(KeyT);
     const uint64_t E = A + (uint64_t)len * sizeof(KeyT);
     const SegCopy ck = seg_copy(A, E, arr_k_lo, arr_k_hi);
-    const uint32_t reg_k = (uint32_t)(ck.e16 - ck.a16);
+    uint32_t reg_k = (uint32_t)(ck.e16 - ck.a16);
+    if constexpr (READ > 0) {
+      // room for the segment's sentinels after its last key
+      const uint32_t need = ((uint32_t)(A - ck.a16) + (uint32_t)(len + READ) * (uint32_t)sizeof(KeyT) + 15u) & ~15u;
+      if (lane < nk && need > reg_k) reg_k = need;
+    }
     int incl = len;
     uint32_t off_k = reg_k;
 #pragma unroll
@@ -835,6 +887,21 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
     // the copied bytes (and its own plain stores) before every other thread's
     // reads.
     constexpr uint32_t kSpinLimit = 1u << 26;
+    // sentinels after every staged segment (the raw-key image of the largest
+    // key when the staged keys are encoded as they are read); written after
+    // the copies land, since a segment's copy may cover its first pad slots
+    // (a rejected tile -- meta[3] < 0 -- has no placement to pad: skipped)
+    auto pad_segments = [&](int l0, int lstep) {
+      if constexpr (READ > 0) {
+        if (d.meta[3] < 0) return;
+        const KeyT sv = a.enc_on_load ? Codec::dec(sentinel_key<KeyT>()) : sentinel_key<KeyT>();
+        KeyT* sk = reinterpret_cast<KeyT*>(stage_k);
+        for (int s = 0; s < nk; ++s) {
+          const int e = d.sbk[s] + (d.cpre[s + 1] - d.cpre[s]);
+          for (int j = l0; j < READ; j += lstep) sk[e + j] = sv;
+        }
+      }
+    };
     if constexpr (COPY == 1) {
       if (warp == 0) {
         const bool ok = mbar_wait_bounded(bar, parity, kSpinLimit);
@@ -842,11 +909,18 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
         if (!ok) {
           if (lane == 0 && a.err) atomicOr(a.err, DEV_COPY_TIMEOUT);
           mbar_wait_bounded(bar, parity, kSpinLimit);  // let copies in flight land
+        } else {
+          __syncwarp();  // lane 0's descriptor writes are visible to the warp
+          pad_segments(lane, 32);
         }
       }
     } else {
       cp_async_wait_all();
       if (tid == 0) *d.status = 0;
+      if constexpr (READ > 0) {
+        __syncthreads();  // every warp's copies have landed
+        pad_segments(tid, NT);
+      }
     }
     __syncthreads();
     if (*d.status) return;
@@ -888,18 +962,20 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
         const int diag = (tid - wt[p]) * ITEMS;
         const int m = min(ITEMS, pe - ps - diag);
         const int na = pm - ps, nb = pe - pm;
+        const int yo = ps + p * PAD;  // this pair's output (PAD apart from the previous pair)
+        constexpr int kCheck = PAD > 0 ? 2 : 1;
         if (lev == 0) {
           // the staged keys are encoded while read only when the round's input
           // is raw caller data (a uniform branch: two specialised loops)
           auto level0 = [&](const auto& ld) {
             const uint32_t A0 = ld.addr(sbk[si]);
             const uint32_t B0 = (si + 1 < nk) ? ld.addr(sbk[si + 1]) : A0 + (uint32_t)na * sizeof(KeyT);
-            const SmemArray<KeyT> yka(k1 + ps + diag);
-            const SmemArray<V> yva(v1 + ps + diag);
+            const SmemArray<KeyT> yka(k1 + yo + diag);
+            const SmemArray<V> yva(v1 + yo + diag);
             const SmemArray<V> sva(reinterpret_cast<const V*>(stage_v));
             const int gen = a.gen_index;
-            merge_window<ITEMS, KeyT, NS>(ld, cmp, A0, na, B0, nb, diag, m, lanes,
-                                          [&](int i, KeyT k, uint32_t src, bool ta) {
+            merge_window<ITEMS, KeyT, NS, kCheck>(ld, cmp, A0, na, B0, nb, diag, m, lanes,
+                                                  [&](int i, KeyT k, uint32_t src, bool ta) {
                                             yka.put(i, k);
                                             if constexpr (kHasVal) {
                                               const int seg = ta ? si : si + 1;
@@ -920,14 +996,28 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
           const V* xv = (cur ? v1 : v0);
           V* yv = (cur ? v0 : v1);
           const PlainLoad<KeyT> ld(xk);
-          const SmemArray<KeyT> yka(yk + ps + diag);
-          const SmemArray<V> xva(xv), yva(yv + ps + diag);
-          merge_window<ITEMS, KeyT, NS>(ld, cmp, ld.addr(ps), na, ld.addr(pm), nb, diag, m, lanes,
-                                        [&](int i, KeyT k, uint32_t src, bool) {
-                                          yka.put(i, k);
-                                          if constexpr (kHasVal)
-                                            yva.put(i, xva.get((int)((src - ld.base) / (uint32_t)sizeof(KeyT))));
-                                        });
+          const SmemArray<KeyT> yka(yk + yo + diag);
+          const SmemArray<V> xva(xv), yva(yv + yo + diag);
+          // input runs: the outputs of pairs 2p and 2p+1 of the level below
+          const uint32_t A0 = ld.addr(ps + 2 * p * PAD);
+          const uint32_t B0 = mi < nk ? ld.addr(pm + (2 * p + 1) * PAD) : A0 + (uint32_t)na * sizeof(KeyT);
+          merge_window<ITEMS, KeyT, NS, kCheck>(ld, cmp, A0, na, B0, nb, diag, m, lanes,
+                                                [&](int i, KeyT k, uint32_t src, bool) {
+                                                  yka.put(i, k);
+                                                  if constexpr (kHasVal)
+                                                    yva.put(i, xva.get((int)((src - ld.base) / (uint32_t)sizeof(KeyT))));
+                                                });
+        }
+      }
+      if constexpr (PAD > 0) {
+        // sentinels after every output pair, read by the next level (the
+        // windows that end a pair spill the same value into the gap)
+        if (span < nk) {
+          KeyT* yk = (cur ? k0 : k1);
+          for (int x = tid; x < np * PAD; x += NT) {
+            const int q = x / PAD;
+            yk[cpre[min(q * span + span, nk)] + q * PAD + (x - q * PAD)] = sentinel_key<KeyT>();
+          }
         }
       }
       __syncthreads();

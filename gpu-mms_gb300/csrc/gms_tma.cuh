@@ -68,6 +68,14 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 
 // Bounded wait.  Returns false if the phase did not complete within the limit
 // (the caller reports it and stops; nothing spins forever).
+//
+// After a timeout the kernels set DEV_COPY_TIMEOUT, wait once more (bounded)
+// so that copies still in flight can land, and then leave the CTA.  If that
+// second wait also runs out, the CTA exits with bulk copies possibly still
+// writing its shared memory, which the PTX memory model leaves undefined;
+// this exit is accepted only because the status bit has already marked the
+// whole result invalid, and the only other choice would be to spin without a
+// bound.  A CTA that timed out issues no further copies.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint32_t limit) {
   for (uint32_t i = 0; i < limit; ++i) {
     if (mbar_try_wait(bar, parity)) return true;

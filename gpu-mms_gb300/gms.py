@@ -14,6 +14,7 @@ squareSort (src/basecase/squareSort.hxx:62-131), one merge round
 from __future__ import annotations
 
 import ctypes
+import hashlib
 import os
 import subprocess
 import threading
@@ -61,12 +62,30 @@ def _sources():
     return out
 
 
+def _source_hash():
+    """SHA-256 over every source file (path and bytes), the compiler flags and
+    the unit list: the build's identity, independent of file times."""
+    h = hashlib.sha256()
+    for p in sorted(_sources()):
+        h.update(os.path.relpath(p, ROOT).encode())
+        with open(p, "rb") as f:
+            h.update(f.read())
+    h.update(repr((NVCC_FLAGS, UNITS)).encode())
+    return h.hexdigest()
+
+
 def build(force=False, jobs=None, verbose=False):
-    """Compile csrc/*.cu for sm_103a into libgms.so (in-tree)."""
+    """Compile csrc/*.cu for sm_103a into libgms.so (in-tree).  Skipped only
+    when libgms.so and the command-line programs exist and were built from
+    sources with the same hash (recorded in _build/sources.sha256)."""
     os.makedirs(BUILD, exist_ok=True)
-    newest = max(os.path.getmtime(p) for p in _sources())
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= newest:
+    digest = _source_hash()
+    stamp = os.path.join(BUILD, "sources.sha256")
+    built = open(stamp).read().strip() if os.path.exists(stamp) else ""
+    if not force and built == digest and all(os.path.exists(p) for p in (LIB, CLI, THRUST)):
         return LIB
+    if os.path.exists(stamp):
+        os.unlink(stamp)
     nvcc = _nvcc()
 
     def compile_one(unit):
@@ -109,6 +128,8 @@ def build(force=False, jobs=None, verbose=False):
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    with open(stamp, "w") as f:
+        f.write(digest + "\n")
     return LIB
 
 
@@ -135,6 +156,7 @@ SIGNATURES = {
     "gms_sort_host_i32_async": (_i32, [_vp, _vp, _i64, _vp]),
     "gms_host_sync": (_i32, [_vp]),
     "gms_sort_i32_noalloc": (_i32, [_vp, _vp, _i64, _vp]),
+    "gms_noalloc_status": (_i32, [_vp, ctypes.POINTER(_i32)]),
     "gms_sort_host_kv_u64_i32": (_i32, [_vp, _vp, _vp, _vp, _i64, _vp]),
     "gms_segmented_sort_i32": (_i32, [_vp, _vp, _i64, _vp, _i64, _vp]),
     "gms_segmented_sort_u32": (_i32, [_vp, _vp, _i64, _vp, _i64, _vp]),

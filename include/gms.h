@@ -107,6 +107,12 @@ int gms_sort_kv_f64_i32(double* keys_in, int32_t* vals_in, double* keys_out, int
  * ------------------------------------------------------------------------- */
 #define GMS_NOALLOC_MAX_N ((int64_t)1 << 22)
 int gms_sort_i32_noalloc(int32_t* input, int32_t* output, int64_t n, void* stream);
+/* Waits for `stream`, then reads and clears the device status word of the
+ * allocation-free sort's static array (the bits of gms_device_status, which
+ * does not see this path: it reads the per-stream scratch instead).  Copies
+ * into a host variable; allocates nothing.  gms_release_workspaces makes the
+ * next call look the array's address up again (needed after a device reset). */
+int gms_noalloc_status(void* stream, int* status_out);
 
 /* ---------------------------------------------------------------------------
  * End-to-end sorts from host memory: copy n keys from `host_in` to the device,
@@ -185,8 +191,8 @@ int gms_find_partitions_i32(const int32_t* task, int64_t size, int k, int64_t ta
  * offsets[nseg] = n (device int64, nseg+1 entries; empty arrays allowed).
  * Every array is sorted into the same range of `output`; `input` is not
  * modified.  One sort of 64-bit (array, key) composites sorts them all: every
- * round is one launch over all arrays.  Bad offsets set bit 3 of the device
- * status word (gms_device_status).
+ * round is one launch over all arrays.  Bad offsets set bit 3 (value 8) of the
+ * device status word (gms_device_status).
  *
  * No counterpart in the reference: GPU-MMS sorts one array per
  * multimergesort call (src/multimergesort.hxx:56-141).
@@ -274,9 +280,17 @@ int gms_sort_ws(int dtype, int kv, void* keys_in, int32_t* vals_in, void* keys_o
 int gms_workspace_status(void* workspace, void* stream, int* status_out);
 
 /* Waits for `stream`, then reads and clears the device status word of the
- * stream's scratch: 0 = no kernel reported a problem; bit 0 = a tile exceeded
- * the shared-memory capacity and was skipped; bit 1 = a tile boundary lay
- * outside its run.  Either bit means the result is wrong (never expected).
+ * stream's scratch: 0 = no kernel reported a problem;
+ *   bit 0 (1) = a tile exceeded the shared-memory capacity and was skipped;
+ *   bit 1 (2) = a tile boundary lay outside its run;
+ *   bit 2 (4) = a bulk copy into shared memory did not complete within the
+ *               spin limit of its wait, and its tile was skipped (any sort,
+ *               merge round or tile sort);
+ *   bit 3 (8) = a batched sort's offsets were not monotone within [0, n].
+ * Bits 0-2 mean the result is wrong (never expected); bit 3 means the caller's
+ * offsets were bad.  Sorts with a caller-provided workspace report in that
+ * workspace (gms_workspace_status), the allocation-free sort in its static
+ * array (gms_noalloc_status).
  * No reference counterpart (the reference reports nothing from its kernels). */
 int gms_device_status(void* stream, int* status_out);
 

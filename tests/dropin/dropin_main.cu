@@ -5,10 +5,12 @@
 // (the drop-in sort is stable).  Prints one line per case; exit code 0 only if
 // every case matches bit for bit.
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <random>
+#include <thread>
 #include <vector>
 
 #include "multimergesort.hxx"
@@ -78,14 +80,68 @@ static void run_case(const char* name, std::vector<T> h, HostLess less, bool fiv
   cudaFree(d_out);
 }
 
+// Several host threads calling multimergesort at the same moment, each on its
+// own arrays, three calls each: the built-in fast path (int, long long) and a
+// user comparator side by side.  Every result must be bit-exact.
+template <class T, int (*f)(T, T), class HostLess>
+static bool thread_sorts(std::vector<T> h, HostLess less, std::atomic<int>* go, int reps) {
+  const int n = (int)h.size();
+  std::vector<T> want = h;
+  std::stable_sort(want.begin(), want.end(), less);
+  T *d_in = nullptr, *d_out = nullptr;
+  if (cudaMalloc(&d_in, sizeof(T) * n) != cudaSuccess || cudaMalloc(&d_out, sizeof(T) * n) != cudaSuccess) return false;
+  go->fetch_add(1);
+  while (go->load() < 3) {
+  }
+  bool ok = true;
+  std::vector<T> got(n);
+  for (int r = 0; r < reps && ok; ++r) {
+    cudaMemcpy(d_in, h.data(), sizeof(T) * n, cudaMemcpyHostToDevice);
+    T* res = multimergesort<T, f>(d_in, d_out, h.data(), n);
+    ok = res != nullptr && cudaMemcpy(got.data(), res, sizeof(T) * n, cudaMemcpyDeviceToHost) == cudaSuccess &&
+         std::memcmp(got.data(), want.data(), sizeof(T) * n) == 0;
+  }
+  cudaFree(d_in);
+  cudaFree(d_out);
+  return ok;
+}
+
+static void concurrent_case(std::mt19937& g) {
+  std::vector<int> a((1 << 22) + 5), c(1000003);
+  std::vector<long long> b(3000017);
+  for (int& x : a) x = (int)g();
+  for (long long& x : b) x = (long long)(((unsigned long long)g() << 32) | g());
+  for (int& x : c) x = (int)(g() % 2001) - 1000;
+  std::atomic<int> go{0};
+  bool ok[3] = {false, false, false};
+  std::thread t0([&] { ok[0] = thread_sorts<int, cmp<int>>(a, [](int x, int y) { return x < y; }, &go, 3); });
+  std::thread t1([&] {
+    ok[1] = thread_sorts<long long, cmp<long long>>(b, [](long long x, long long y) { return x < y; }, &go, 3);
+  });
+  std::thread t2([&] { ok[2] = thread_sorts<int, desc_cmp>(c, [](int x, int y) { return x > y; }, &go, 3); });
+  t0.join();
+  t1.join();
+  t2.join();
+  const bool all = ok[0] && ok[1] && ok[2];
+  printf("%-28s %s\n", "3 host threads at once", all ? "OK" : "MISMATCH");
+  if (!all) ++failures;
+}
+
 int main() {
   std::mt19937 g(1234);
-  const int sizes[] = {0, 1, 7, 1000, 4352, 4353, 300001, (1 << 22) + 3};
+  const int sizes[] = {0, 1, 7, 1000, 4352, 4353, 8193, 300001, (1 << 22) + 3, 1 << 24};
   for (int n : sizes) {
     std::vector<int> a(n);
     for (int& x : a) x = (int)(g() % 2001) - 1000;  // many ties
     run_case<int, cmp<int>>("default cmp<int> (4 args)", a, [](int x, int y) { return x < y; }, false);
     run_case<int, cmp<int>>("default cmp<int> (5 args)", a, [](int x, int y) { return x < y; }, true);
+    std::vector<unsigned> u(n);
+    for (unsigned& x : u) x = (unsigned)g();
+    run_case<unsigned, cmp<unsigned>>("default cmp<unsigned>", u, [](unsigned x, unsigned y) { return x < y; }, false);
+    std::vector<long long> ll(n);
+    for (long long& x : ll) x = (long long)(((unsigned long long)g() << 32) | g());
+    run_case<long long, cmp<long long>>("default cmp<long long>", ll, [](long long x, long long y) { return x < y; },
+                                        false);
     run_case<int, desc_cmp>("descending", a, [](int x, int y) { return x > y; }, false);
     run_case<int, abs_cmp>("absolute value (stable)", a, [](int x, int y) { return std::abs(x) < std::abs(y); }, false);
     std::vector<Rec> r(n);
@@ -110,6 +166,7 @@ int main() {
   std::vector<int> ext(100003);
   for (int& x : ext) x = (g() & 1) ? MAXVAL : (int)(g() % 5) - 2;
   run_case<int, cmp<int>>("MAXVAL keys", ext, [](int x, int y) { return x < y; }, false);
+  concurrent_case(g);
   printf(failures ? "DROPIN FAILED\n" : "DROPIN OK\n");
   return failures ? 1 : 0;
 }
