@@ -4,6 +4,7 @@
 #include <vector>
 
 #include "gms_capi.cuh"
+#include "gms_capi_seg.cuh"
 
 using namespace gms_capi;
 using gms::NoVal;
@@ -260,6 +261,23 @@ void gms_capi::release_host_pipes() {
   g_pipes.clear();
 }
 
+int gms_capi::seg_prepare_i32(const std::vector<int64_t>& off, int64_t nseg, const gms::Tune& t, SegJob* job) {
+  return seg_prepare<EngI32, uint32_t>(off, nseg, t, job);
+}
+
+cudaError_t gms_capi::seg_sort_i32(const SegJob& job, void* ws, const int32_t* in, int32_t* tmp, int32_t* out,
+                                   int64_t n, const gms::Tune& t, cudaStream_t st) {
+  const gms::WsPtrs<uint32_t> w = gms::ws_carve<uint32_t>(gms::seg_ws_layout(job.plan), t.k, ws);
+  return EngI32::seg_sort(w, job.dev, (const uint32_t*)in, nullptr, (uint32_t*)tmp, nullptr, (uint32_t*)out, nullptr,
+                          n, t, st);
+}
+
+int gms_capi::seg_run_i32(SegJob* job, const void* dblob, const int32_t* in, int32_t* out, int64_t n,
+                          const gms::Tune& t, cudaStream_t st) {
+  return run_planned<EngI32, uint32_t, NoVal>(job, dblob, (const uint32_t*)in, nullptr, (uint32_t*)out, nullptr, n, t,
+                                              st);
+}
+
 int gms_capi::sort32_ws(int dtype, void* in, void* out, int64_t n, void* ws, size_t bytes, cudaStream_t st) {
   uint32_t* i = (uint32_t*)in;
   uint32_t* o = (uint32_t*)out;
@@ -360,6 +378,19 @@ int gms_sort_host_i32(const int32_t* host_in, int32_t* host_out, int64_t n, void
   const int status = host_sort_enqueue(host_in, host_out, n, (cudaStream_t)stv, true);
   if (status != GMS_OK) return status;
   return host_sync((cudaStream_t)stv);
+}
+
+int gms_segmented_sort_i32(const int32_t* in, int32_t* out, int64_t n, const int64_t* offsets, int64_t nseg, void* st) {
+  return run_segmented<EngI32, uint32_t, NoVal>((const uint32_t*)in, nullptr, (uint32_t*)out, nullptr, n, offsets, nseg,
+                                                (cudaStream_t)st, 0);
+}
+int gms_segmented_sort_u32(const uint32_t* in, uint32_t* out, int64_t n, const int64_t* offsets, int64_t nseg,
+                           void* st) {
+  return run_segmented<EngU32, uint32_t, NoVal>(in, nullptr, out, nullptr, n, offsets, nseg, (cudaStream_t)st, 1);
+}
+int gms_segmented_sort_f32(const float* in, float* out, int64_t n, const int64_t* offsets, int64_t nseg, void* st) {
+  return run_segmented<EngF32, uint32_t, NoVal>((const uint32_t*)in, nullptr, (uint32_t*)out, nullptr, n, offsets, nseg,
+                                                (cudaStream_t)st, 2);
 }
 
 }  // extern "C"

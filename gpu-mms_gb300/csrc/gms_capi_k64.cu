@@ -1,5 +1,6 @@
 // C ABI: 64-bit keys (int64, uint64, float64), keys only.
 #include "gms_capi.cuh"
+#include "gms_capi_seg.cuh"
 
 using namespace gms_capi;
 using gms::NoVal;
@@ -66,6 +67,19 @@ int gms_merge_level_u64(const uint64_t* in, uint64_t* out, int64_t n, int64_t ru
   const gms::WsPtrs<uint64_t> w = gms::ws_carve<uint64_t>(l, k, ws);
   cudaError_t e = EngU64::merge_level(w, in, out, n, run_len, t, (cudaStream_t)st);
   return e == cudaSuccess ? GMS_OK : cuda_error(e, "merge_level");
+}
+
+int gms_segmented_sort_i64(const int64_t* in, int64_t* out, int64_t n, const int64_t* offsets, int64_t nseg, void* st) {
+  return run_segmented<EngI64, uint64_t, NoVal>((const uint64_t*)in, nullptr, (uint64_t*)out, nullptr, n, offsets, nseg,
+                                                (cudaStream_t)st, 3);
+}
+int gms_segmented_sort_u64(const uint64_t* in, uint64_t* out, int64_t n, const int64_t* offsets, int64_t nseg,
+                           void* st) {
+  return run_segmented<EngU64, uint64_t, NoVal>(in, nullptr, out, nullptr, n, offsets, nseg, (cudaStream_t)st, 4);
+}
+int gms_segmented_sort_f64(const double* in, double* out, int64_t n, const int64_t* offsets, int64_t nseg, void* st) {
+  return run_segmented<EngF64, uint64_t, NoVal>((const uint64_t*)in, nullptr, (uint64_t*)out, nullptr, n, offsets, nseg,
+                                                (cudaStream_t)st, 5);
 }
 
 }  // extern "C"

@@ -1,5 +1,6 @@
 // C ABI: key/value sorts (stable), int32 payload.
 #include "gms_capi.cuh"
+#include "gms_capi_seg.cuh"
 
 using namespace gms_capi;
 
@@ -11,6 +12,16 @@ int kv(void* ki, int32_t* vi, void* ko, int32_t* vo, int64_t n, void* st, int dt
 }
 
 }  // namespace
+
+int gms_capi::seg_prepare_kv_u64(const std::vector<int64_t>& off, int64_t nseg, const gms::Tune& t, SegJob* job) {
+  return seg_prepare<KvEngine<uint64_t, gms::IdentityCodec<uint64_t>>, uint64_t>(off, nseg, t, job);
+}
+
+int gms_capi::seg_run_kv_u64(SegJob* job, const void* dblob, const uint64_t* kin, const int32_t* vin, uint64_t* kout,
+                             int32_t* vout, int64_t n, const gms::Tune& t, cudaStream_t st) {
+  return run_planned<KvEngine<uint64_t, gms::IdentityCodec<uint64_t>>, uint64_t, int32_t>(job, dblob, kin, vin, kout,
+                                                                                        vout, n, t, st);
+}
 
 int gms_capi::sort_kv_ws(int dtype, void* ki, int32_t* vi, void* ko, int32_t* vo, int64_t n, void* ws, size_t bytes,
                          cudaStream_t st) {
@@ -86,6 +97,37 @@ int gms_sort_host_kv_u64_i32(const uint64_t* keys_in, const int32_t* vals_in, ui
   if (e != cudaSuccess) return cuda_error(e, "cudaMemcpyAsync D2H");
   e = cudaStreamSynchronize(st);
   return e == cudaSuccess ? GMS_OK : cuda_error(e, "cudaStreamSynchronize");
+}
+
+int gms_segmented_sort_kv_i32_i32(const int32_t* ki, const int32_t* vi, int32_t* ko, int32_t* vo, int64_t n,
+                                  const int64_t* offsets, int64_t nseg, void* st) {
+  return run_segmented<KvEngine<uint32_t, gms::SignFlip32>, uint32_t, int32_t>(
+      (const uint32_t*)ki, vi, (uint32_t*)ko, vo, n, offsets, nseg, (cudaStream_t)st, 0);
+}
+int gms_segmented_sort_kv_u32_i32(const uint32_t* ki, const int32_t* vi, uint32_t* ko, int32_t* vo, int64_t n,
+                                  const int64_t* offsets, int64_t nseg, void* st) {
+  return run_segmented<KvEngine<uint32_t, gms::IdentityCodec<uint32_t>>, uint32_t, int32_t>(
+      ki, vi, ko, vo, n, offsets, nseg, (cudaStream_t)st, 1);
+}
+int gms_segmented_sort_kv_f32_i32(const float* ki, const int32_t* vi, float* ko, int32_t* vo, int64_t n,
+                                  const int64_t* offsets, int64_t nseg, void* st) {
+  return run_segmented<KvEngine<uint32_t, gms::FloatOrder32>, uint32_t, int32_t>(
+      (const uint32_t*)ki, vi, (uint32_t*)ko, vo, n, offsets, nseg, (cudaStream_t)st, 2);
+}
+int gms_segmented_sort_kv_i64_i32(const int64_t* ki, const int32_t* vi, int64_t* ko, int32_t* vo, int64_t n,
+                                  const int64_t* offsets, int64_t nseg, void* st) {
+  return run_segmented<KvEngine<uint64_t, gms::SignFlip64>, uint64_t, int32_t>(
+      (const uint64_t*)ki, vi, (uint64_t*)ko, vo, n, offsets, nseg, (cudaStream_t)st, 3);
+}
+int gms_segmented_sort_kv_u64_i32(const uint64_t* ki, const int32_t* vi, uint64_t* ko, int32_t* vo, int64_t n,
+                                  const int64_t* offsets, int64_t nseg, void* st) {
+  return run_segmented<KvEngine<uint64_t, gms::IdentityCodec<uint64_t>>, uint64_t, int32_t>(
+      ki, vi, ko, vo, n, offsets, nseg, (cudaStream_t)st, 4);
+}
+int gms_segmented_sort_kv_f64_i32(const double* ki, const int32_t* vi, double* ko, int32_t* vo, int64_t n,
+                                  const int64_t* offsets, int64_t nseg, void* st) {
+  return run_segmented<KvEngine<uint64_t, gms::FloatOrder64>, uint64_t, int32_t>(
+      (const uint64_t*)ki, vi, (uint64_t*)ko, vo, n, offsets, nseg, (cudaStream_t)st, 5);
 }
 
 }  // extern "C"

@@ -319,10 +319,9 @@ int gms_reserve(int dtype, int kv, int64_t n, void* stream) {
   if (dtype < 0 || dtype > GMS_RESERVE_SEGMENTED_I32 || n < 0) return set_error(GMS_ERR_INVALID, "bad dtype or n");
   int status = GMS_OK;
   if (dtype == GMS_RESERVE_SEGMENTED_I32) {
-    // the 64-bit composite sort's scratch and its two composite buffers
-    cache_get(0, gms_workspace_bytes(4, 0, n), (cudaStream_t)stream, &status);
-    if (status == GMS_OK) cache_get(30, sizeof(uint64_t) * (size_t)(n > 0 ? n : 1), (cudaStream_t)stream, &status);
-    if (status == GMS_OK) cache_get(31, sizeof(uint64_t) * (size_t)(n > 0 ? n : 1), (cudaStream_t)stream, &status);
+    // a plain sort's scratch and the batched sort's scratch array of n keys
+    cache_get(0, gms_workspace_bytes(0, 0, n), (cudaStream_t)stream, &status);
+    if (status == GMS_OK) cache_get(30, sizeof(uint32_t) * (size_t)(n > 0 ? n : 1), (cudaStream_t)stream, &status);
     return status;
   }
   cache_get(0, gms_workspace_bytes(dtype, kv, n), (cudaStream_t)stream, &status);

@@ -1,65 +1,49 @@
-// C ABI: batched (segmented) sorts and CUDA-graph capture of a sort.
+// C ABI: host side of the batched (segmented) sorts, and CUDA-graph capture of
+// a sort.  The batched entry points themselves sit with the plain sorts of
+// their key type (gms_capi_k32.cu, gms_capi_k64.cu, gms_capi_kv.cu), whose
+// kernels they share.
 #include <new>
+#include <vector>
 
-#include "gms_capi.cuh"
-#include "gms_segmented.cuh"
+#include "gms_capi_seg.cuh"
 
 using namespace gms_capi;
 
-namespace {
+namespace gms_capi {
 
-using CompEngine = KeysEngine<uint64_t, gms::IdentityCodec<uint64_t>>;
-
-// Flags the status word if the offsets are not 0 = off[0] <= ... <= off[nseg] = n.
-__global__ void check_offsets_kernel(const int64_t* __restrict__ off, int64_t nseg, int64_t n, int* err) {
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < nseg; s += stride) {
-    const bool bad = off[s] > off[s + 1] || (s == 0 && off[0] != 0) || (s == nseg - 1 && off[nseg] != n);
-    if (bad && err) atomicOr(err, 8);
+int read_offsets(const int64_t* off, int64_t nseg, int64_t n, cudaStream_t st, std::vector<int64_t>* h) {
+  h->assign((size_t)nseg + 1, 0);
+  cudaError_t e = cudaMemcpyAsync(h->data(), off, sizeof(int64_t) * (size_t)(nseg + 1), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_error(e, "reading the offsets");
+  const std::vector<int64_t>& o = *h;
+  if (o[0] != 0 || o[(size_t)nseg] != n) return set_error(GMS_ERR_INVALID, "offsets must start at 0 and end at n");
+  for (int64_t s = 0; s < nseg; ++s) {
+    if (o[(size_t)s + 1] < o[(size_t)s]) return set_error(GMS_ERR_INVALID, "offsets must not decrease");
   }
-}
-
-template <class Codec32>
-int segmented32(void* in, void* out, int64_t n, const int64_t* off, int64_t nseg, cudaStream_t st) {
-  clear_error();
-  if (n < 0 || nseg < 0) return set_error(GMS_ERR_INVALID, "n < 0 or nseg < 0");
-  if (n == 0 || nseg == 0) return GMS_OK;
-  if (!in || !out || !off) return set_error(GMS_ERR_INVALID, "null pointer");
-  if (nseg > 0xffffffffll) return set_error(GMS_ERR_TOO_LARGE, "more than 2^32 segments");
-  if (n > ((int64_t)1 << 37)) return set_error(GMS_ERR_TOO_LARGE, "n beyond 2^37");
-  const gms::Tune t = tune_for(4, 0, n);  // the composites sort as uint64 keys
-  const gms::WsLayout l = CompEngine::plan(n, t);
-  if (!l.ok) return set_error(GMS_ERR_INVALID, "tuning too fine for this n (sample recursion too deep)");
-  int status = GMS_OK;
-  void* ws = cache_get(0, gms::ws_bytes_for<uint64_t>(l, t.k), st, &status);
-  if (status != GMS_OK) return status;
-  const gms::WsPtrs<uint64_t> w = gms::ws_carve<uint64_t>(l, t.k, ws);
-  uint64_t* ca = (uint64_t*)cache_get(30, sizeof(uint64_t) * (size_t)n, st, &status);
-  if (status != GMS_OK) return status;
-  uint64_t* cb = (uint64_t*)cache_get(31, sizeof(uint64_t) * (size_t)n, st, &status);
-  if (status != GMS_OK) return status;
-  check_offsets_kernel<<<(unsigned)gms::ceil_div(nseg, 256) > 4096 ? 4096 : (unsigned)gms::ceil_div(nseg, 256), 256, 0,
-                         st>>>(off, nseg, n, w.err);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return cuda_error(e, "check_offsets_kernel");
-  gms::build_composite_kernel<Codec32>
-      <<<(unsigned)gms::ceil_div(n, gms::kSegChunk), gms::kSegThreads, 0, st>>>((const uint32_t*)in, off, nseg, n, ca);
-  if ((e = cudaGetLastError()) != cudaSuccess) return cuda_error(e, "build_composite_kernel");
-  e = CompEngine::sort(w, ca, nullptr, cb, nullptr, n, t, st);
-  if (e != cudaSuccess) return cuda_error(e, "segmented sort");
-  const int64_t blocks = gms::ceil_div(n, 1024) < 65536 ? gms::ceil_div(n, 1024) : 65536;
-  gms::extract_composite_kernel<Codec32><<<(unsigned)blocks, 256, 0, st>>>(cb, (uint32_t*)out, n);
-  if ((e = cudaGetLastError()) != cudaSuccess) return cuda_error(e, "extract_composite_kernel");
   return GMS_OK;
 }
 
-}  // namespace
+int seg_upload(SegJob* job, void* dblob, cudaStream_t st) {
+  std::vector<unsigned char> host(job->blob.bytes);
+  gms::seg_blob_fill(job->plan, job->blob, host.data());
+  // from pageable memory: the call returns once the bytes are staged, so the
+  // host buffer may go right after it
+  const cudaError_t e = cudaMemcpyAsync(dblob, host.data(), job->blob.bytes, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return cuda_error(e, "uploading the batch plan");
+  gms::seg_bind(job->plan, job->blob, dblob, &job->dev);
+  return GMS_OK;
+}
+
+}  // namespace gms_capi
 
 // ---------------------------------------------------------------------------
 // CUDA graphs
 struct gms_graph {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
+  std::vector<void*> owned;        // device buffers the captured launches use
+  gms_capi::SegJob* job = nullptr;  // plan of a captured batched sort
 };
 
 namespace {
@@ -111,16 +95,6 @@ int capture(cudaStream_t st, gms_graph** out, F&& body) {
 
 extern "C" {
 
-int gms_segmented_sort_i32(int32_t* in, int32_t* out, int64_t n, const int64_t* offsets, int64_t nseg, void* st) {
-  return segmented32<gms::SignFlip32>(in, out, n, offsets, nseg, (cudaStream_t)st);
-}
-int gms_segmented_sort_u32(uint32_t* in, uint32_t* out, int64_t n, const int64_t* offsets, int64_t nseg, void* st) {
-  return segmented32<gms::IdentityCodec<uint32_t>>(in, out, n, offsets, nseg, (cudaStream_t)st);
-}
-int gms_segmented_sort_f32(float* in, float* out, int64_t n, const int64_t* offsets, int64_t nseg, void* st) {
-  return segmented32<gms::FloatOrder32>(in, out, n, offsets, nseg, (cudaStream_t)st);
-}
-
 int gms_graph_create_sort_i32(int32_t* in, int32_t* out, int64_t n, void* stream, gms_graph** graph) {
   clear_error();
   cudaStream_t st = (cudaStream_t)stream;
@@ -133,7 +107,45 @@ int gms_graph_create_segmented_i32(int32_t* in, int32_t* out, int64_t n, const i
   clear_error();
   cudaStream_t st = (cudaStream_t)stream;
   if (!st) return set_error(GMS_ERR_INVALID, "graph capture needs a non-default stream");
-  return capture(st, graph, [&]() { return gms_segmented_sort_i32(in, out, n, offsets, nseg, stream); });
+  if (!graph) return set_error(GMS_ERR_INVALID, "null graph handle");
+  *graph = nullptr;
+  if (n <= 0 || nseg <= 0 || !in || !out || !offsets) return set_error(GMS_ERR_INVALID, "empty batch or null pointer");
+  // The plan, its device arrays, the scratch and the scratch array of n keys
+  // belong to the graph (not to the per-stream cache, whose buffers a later
+  // call may regrow), so the captured launches stay valid until it is destroyed.
+  std::vector<int64_t> h;
+  int status = read_offsets(offsets, nseg, n, st, &h);
+  if (status != GMS_OK) return status;
+  const gms::Tune t = tune_for(0, 0, n);
+  SegJob* job = new (std::nothrow) SegJob;
+  if (!job) return set_error(GMS_ERR_NOMEM, "graph plan");
+  status = seg_prepare_i32(h, nseg, t, job);
+  void* blob = nullptr;
+  void* ws = nullptr;
+  void* tmp = nullptr;
+  auto fail = [&](int st2) {
+    cudaFree(blob);
+    cudaFree(ws);
+    cudaFree(tmp);
+    delete job;
+    return st2;
+  };
+  if (status != GMS_OK) return fail(status);
+  cudaError_t e = cudaMalloc(&blob, job->blob.bytes);
+  if (e == cudaSuccess) e = cudaMalloc(&ws, job->ws_bytes);
+  if (e == cudaSuccess) e = cudaMalloc(&tmp, sizeof(uint32_t) * (size_t)n);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ws, 0, 256, st);
+  if (e != cudaSuccess) return fail(cuda_error(e, "graph buffers"));
+  status = seg_upload(job, blob, st);
+  if (status != GMS_OK) return fail(status);
+  status = capture(st, graph, [&]() {
+    const cudaError_t ee = seg_sort_i32(*job, ws, in, (int32_t*)tmp, out, n, t, st);
+    return ee == cudaSuccess ? GMS_OK : cuda_error(ee, "segmented sort");
+  });
+  if (status != GMS_OK) return fail(status);
+  (*graph)->owned = {blob, ws, tmp};
+  (*graph)->job = job;
+  return GMS_OK;
 }
 
 int gms_graph_launch(gms_graph* graph, void* stream) {
@@ -148,6 +160,8 @@ int gms_graph_destroy(gms_graph* graph) {
   if (!graph) return GMS_OK;
   if (graph->exec) cudaGraphExecDestroy(graph->exec);
   if (graph->graph) cudaGraphDestroy(graph->graph);
+  for (void* p : graph->owned) cudaFree(p);
+  delete graph->job;
   delete graph;
   return GMS_OK;
 }

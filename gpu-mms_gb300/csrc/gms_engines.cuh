@@ -17,9 +17,9 @@ namespace gms_engines {
 // keys with int32 payload):
 //   keys only   base: warp-shuffle base case (8192-key tiles for 32-bit
 //               keys, 4096 for 64-bit keys); 512 x 17 for tile_sort; data
-//               rounds 288 x 31 with one merge stream per window (32-bit
-//               keys: three CTAs of ~76 KB shared memory per SM, runs padded
-//               with sentinels) or 256 x 17 (64-bit keys)
+//               rounds with one merge stream per window and runs padded with
+//               sentinels: 288 x 31 (32-bit keys: three CTAs of ~76 KB shared
+//               memory per SM) or 256 x 17 (64-bit keys)
 //   key/value   base and data rounds 256 x 17 (keys + payload staged: three
 //               CTAs per SM for 32-bit keys)
 //   index rounds (a block sample merged with its uint32 positions) 256 x 17,
@@ -28,7 +28,7 @@ constexpr int kNT = 512;
 constexpr int kItems = 17;
 using IndexGeo = gms::MergeGeo<256, 17>;
 template <class Key>
-using KeysGeo = std::conditional_t<sizeof(Key) == 4, gms::MergeGeo<288, 31, 1>, gms::MergeGeo<256, 17>>;
+using KeysGeo = std::conditional_t<sizeof(Key) == 4, gms::MergeGeo<288, 31, 1>, gms::MergeGeo<256, 17, 1>>;
 // keys-only 32-bit sorts: index rounds of 512 x 17, so a first-round group's
 // block sample (32 runs x 256 entries) is merged by one CTA
 template <class Key>

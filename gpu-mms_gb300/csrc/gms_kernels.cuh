@@ -22,6 +22,22 @@ namespace gms {
 
 enum TileMode : int { MODE_BASE = 0, MODE_GROUP = 1, MODE_TILE = 2 };
 
+// A group of one round of a segmented (batched) sort.  Groups of such a round
+// are listed instead of being K consecutive runs of L keys counted from the
+// array start, so that no group crosses a segment: group g covers keys
+// [start, start + len) (runs of L keys, the last possibly short), its first
+// input run has the global index run0 (block samples of run r sit at
+// r * ceil(L / sample_b)), its forecast tiles are [tile0, next tile0), its
+// boundary rows [row0, next row0).  flags bit 0: the group reads and writes
+// the second buffer pair (in2/out2) of the launch; bit 1: the group's keys are
+// decoded as they are stored (its segment's last round).  A list of G groups
+// has G + 1 entries; the last one holds the totals (tile0, row0).
+// For the base case the groups are the tiles (one run each).
+struct GroupDesc {
+  int64_t start, len, run0, tile0, row0, flags;
+};
+enum GroupFlags : int64_t { GRP_ALT = 1, GRP_DEC = 2 };
+
 // Arguments of one launch of tile_kernel.
 template <class KeyT, class V>
 struct TileArgs {
@@ -49,6 +65,14 @@ struct TileArgs {
   int dec_on_store;  // apply Codec::dec to stored keys
   int gen_index;     // payload = input position (uint32), ignoring vin
   int* err;          // device status word (bit 0: tile over capacity); may be null
+  // segmented rounds: groups listed in grp (null: regular groups), the group
+  // of every forecast tile, and the second buffer pair of GRP_ALT groups
+  const GroupDesc* grp;
+  const int32_t* tile_grp;
+  const KeyT* in2;
+  KeyT* out2;
+  const V* vin2;
+  V* vout2;
 };
 
 // Bits of the device status word.
@@ -73,6 +97,19 @@ struct TileSmemLayout {
 };
 
 __device__ __forceinline__ int64_t min64(int64_t a, int64_t b) { return a < b ? a : b; }
+
+// Arguments of one group of a segmented round: the buffer pair its flags
+// select and, for its segment's last round, decoding on store.
+template <class KeyT, class V>
+__device__ __forceinline__ void use_group(TileArgs<KeyT, V>& a, int64_t flags) {
+  if (flags & GRP_ALT) {
+    a.in = a.in2;
+    a.out = a.out2;
+    a.vin = a.vin2;
+    a.vout = a.vout2;
+  }
+  if (flags & GRP_DEC) a.dec_on_store = 1;
+}
 
 template <class Codec, class KeyT>
 __device__ __forceinline__ KeyT maybe_enc(KeyT x, int on) {
@@ -104,9 +141,15 @@ struct EncCmp {
 //   MODE_TILE : CTA merges one tile of a group whose runs are cut by `desc`.
 // STABLE: equivalent keys keep their input order (used for key/value sorts and
 // for user comparators whose equivalent keys may differ in their bits).
+// With a.grp (segmented rounds) CTA g takes group g: MODE_BASE sorts the tile
+// [start, start + len), MODE_GROUP merges the group's runs; MODE_TILE is not
+// used with listed groups.
 template <class KeyT, class V, class Cmp, class Codec, int MODE, bool STABLE, int NT, int ITEMS>
 __global__ void __launch_bounds__(NT, (MODE == MODE_BASE && sizeof(KeyT) == 4 && !HasVal<V>::value) ? 3 : 1)
-    tile_kernel(TileArgs<KeyT, V> a) {
+    tile_kernel(TileArgs<KeyT, V> a0) {
+  TileArgs<KeyT, V> a = a0;
+  const GroupDesc* gd = a.grp ? a.grp + blockIdx.x : nullptr;
+  if (gd) use_group(a, gd->flags);
   constexpr int CAP = NT * ITEMS;
   constexpr bool kHasVal = HasVal<V>::value;
   using Lay = TileSmemLayout<KeyT, V, CAP>;
@@ -131,9 +174,9 @@ __global__ void __launch_bounds__(NT, (MODE == MODE_BASE && sizeof(KeyT) == 4 &&
   const int s = tid * ITEMS;
 
   if constexpr (MODE == MODE_BASE) {
-    const int64_t base = (int64_t)blockIdx.x * a.L;
+    const int64_t base = gd ? gd->start : (int64_t)blockIdx.x * a.L;
     if (base >= a.n) return;
-    cnt = (int)min64(a.L, a.n - base);
+    cnt = gd ? (int)gd->len : (int)min64(a.L, a.n - base);
     out_base = base;
     run_base = base;
     run_index = blockIdx.x;
@@ -265,9 +308,9 @@ __global__ void __launch_bounds__(NT, (MODE == MODE_BASE && sizeof(KeyT) == 4 &&
     int64_t g;
     if constexpr (MODE == MODE_GROUP) {
       g = blockIdx.x;
-      gbase = g * a.L * a.k;
+      gbase = gd ? gd->start : g * a.L * a.k;
       if (gbase >= a.n) return;
-      const int64_t ng = min64(a.L * a.k, a.n - gbase);
+      const int64_t ng = gd ? gd->len : min64(a.L * a.k, a.n - gbase);
       cnt = (int)ng;
       nk = a.k;
       if (tid <= nk) pre[tid] = (int)min64((int64_t)tid * a.L, ng);
@@ -407,8 +450,13 @@ struct BaseWarpSmem {
 // Runs in shared memory are padded with PAD sentinel keys (the largest key)
 // when the order allows it (RunPad), so the merge levels step without run-end
 // checks; the pad after each run is refilled at every level.
+// With a.grp (segmented sorts) CTA t sorts the tile [start, start + len) of
+// group (tile) t.
 template <class KeyT, class Cmp, class Codec, int NT, int KPL, int ITEMS_M, int NSB = 2>
-__global__ void __launch_bounds__(NT) base_warp_kernel(TileArgs<KeyT, NoVal> a) {
+__global__ void __launch_bounds__(NT) base_warp_kernel(TileArgs<KeyT, NoVal> a0) {
+  TileArgs<KeyT, NoVal> a = a0;
+  const GroupDesc* gd = a.grp ? a.grp + blockIdx.x : nullptr;
+  if (gd) use_group(a, gd->flags);
   constexpr int PAD = RunPad<KeyT, NoVal, Cmp, ITEMS_M, NSB>::gap;
   using Geo = BaseWarpGeom<NT, KPL, ITEMS_M, PAD>;
   constexpr int TILE = Geo::TILE;
@@ -420,9 +468,9 @@ __global__ void __launch_bounds__(NT) base_warp_kernel(TileArgs<KeyT, NoVal> a) 
   const int tid = threadIdx.x;
   const int lane = tid & 31;
   const int warp = tid >> 5;
-  const int64_t base = (int64_t)blockIdx.x * TILE;
+  const int64_t base = gd ? gd->start : (int64_t)blockIdx.x * TILE;
   if (base >= a.n) return;
-  const int cnt = (int)min64(TILE, a.n - base);
+  const int cnt = gd ? (int)gd->len : (int)min64(TILE, a.n - base);
 
   // Load: register i of thread t holds element t + i*NT.  A full tile at a
   // 16-byte-aligned address arrives by one bulk copy (TMA) into the second
@@ -569,12 +617,12 @@ struct MergeSmemLayout {
   static constexpr size_t off_mk = off_stage_v + stage_v_bytes;
   static constexpr size_t off_mv = off_mk + mk_bytes;
   // SETS descriptor sets, one per tile in flight: cpre[33] int, sbk[32] int,
-  // sbv[32] int, a status word, gsrc[32] int64, meta[4] int64, wst[kLevels][17]
+  // sbv[32] int, a status word, gsrc[32] int64, meta[6] int64, wst[kLevels][17]
   // int (first thread of each pair's windows, per level); then the mbarrier.
   static constexpr int kLevels = 5;  // log2(kMaxK)
   static constexpr size_t set_gsrc = 400;
   static constexpr size_t set_meta = set_gsrc + 8 * 32;
-  static constexpr size_t set_wst = set_meta + 8 * 4;
+  static constexpr size_t set_wst = set_meta + 8 * 6;
   static constexpr size_t set_bytes = round16(set_wst + 4 * kLevels * 17);
   static constexpr size_t off_desc = off_mv + mv_bytes;
   static constexpr size_t off_bar = off_desc + SETS * set_bytes;
@@ -596,7 +644,7 @@ struct TileDesc {
   int* sbv;       // ... in the staged payload
   int* status;    // 1: the copy wait timed out
   int64_t* gsrc;  // global index of segment s's first key
-  int64_t* meta;  // output offset, run base, run index, key count (-1: rejected)
+  int64_t* meta;  // output offset, run base, run index, key count (-1: rejected), group flags
   int* wst;       // window tables
   __device__ __forceinline__ TileDesc(unsigned char* base, size_t set_gsrc, size_t set_meta, size_t set_wst)
       : cpre(reinterpret_cast<int*>(base)),
@@ -655,9 +703,32 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
   // tiles of this launch: [a.tile_base, total_tiles); indices past a group's
   // last tile are empty
   auto real_tile = [&](int64_t t) {
+    if (a.grp) return true;  // listed groups: tiles are numbered without gaps
     const int64_t g = t / a.tiles_full;
     const int64_t j = t - g * a.tiles_full;
     return j < ((g == a.groups - 1) ? a.tiles_last : a.tiles_full);
+  };
+  // tile t's group, boundary row, keys and group flags
+  struct TileLoc {
+    int64_t g, row, gbase, ng, flags;
+  };
+  auto locate = [&](int64_t t) {
+    TileLoc l;
+    if (a.grp) {
+      l.g = a.tile_grp[t];
+      const GroupDesc& gd = a.grp[l.g];
+      l.row = gd.row0 + (t - gd.tile0);
+      l.gbase = gd.start;
+      l.ng = gd.len;
+      l.flags = gd.flags;
+    } else {
+      l.g = t / a.tiles_full;
+      l.row = l.g * (a.tiles_full + 1) + (t - l.g * a.tiles_full);
+      l.gbase = l.g * a.L * a.k;
+      l.ng = min64(a.L * a.k, a.n - l.gbase);
+      l.flags = 0;
+    }
+    return l;
   };
   auto next_tile = [&](int64_t t) {
     if (!PERSIST) return total_tiles;
@@ -691,8 +762,7 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
   };
   auto load_bounds = [&](int64_t t) {
     Bounds b;
-    const int64_t g = t / a.tiles_full;
-    const int64_t row = g * (a.tiles_full + 1) + (t - g * a.tiles_full);
+    const int64_t row = locate(t).row;
     if (lane < nk) {
       b.lo = a.desc[row * nk + lane];
       b.hi = a.desc[(row + 1) * nk + lane];
@@ -701,10 +771,14 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
     return b;
   };
   auto stage = [&](int64_t t, const TileDesc& d, const Bounds& bd) {
-    const int64_t g = t / a.tiles_full;
-    const int64_t gbase = g * a.L * a.k;
-    const int64_t ng = min64(a.L * a.k, a.n - gbase);
-    const uint64_t arr_k_lo = reinterpret_cast<uint64_t>(a.in);
+    const TileLoc loc = locate(t);
+    const int64_t g = loc.g;
+    const int64_t gbase = loc.gbase;
+    const int64_t ng = loc.ng;
+    const bool alt = (loc.flags & GRP_ALT) != 0;
+    const KeyT* kin = alt ? a.in2 : a.in;
+    const V* vin = alt ? a.vin2 : a.vin;
+    const uint64_t arr_k_lo = reinterpret_cast<uint64_t>(kin);
     const uint64_t arr_k_hi = arr_k_lo + (uint64_t)a.n * sizeof(KeyT);
     const int64_t lo = bd.lo, hi = bd.hi, out_off = bd.out_off;
     int len = 0;
@@ -747,7 +821,7 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
     const bool carry = kHasVal && !a.gen_index;
     if constexpr (kHasVal) {
       if (carry) {
-        const uint64_t arr_v_lo = reinterpret_cast<uint64_t>(a.vin);
+        const uint64_t arr_v_lo = reinterpret_cast<uint64_t>(vin);
         const uint64_t arr_v_hi = arr_v_lo + (uint64_t)a.n * sizeof(V);
         Av = arr_v_lo + (uint64_t)gs * sizeof(V);
         const uint64_t Ev = Av + (uint64_t)len * sizeof(V);
@@ -813,7 +887,7 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
       unsigned char* dstk = stage_k + off_k;
       // plain loads for bytes outside the array's 16-byte-aligned interior
       // (never more than 15 bytes at each end of the array)
-      const KeyT* src = a.in + gs;
+      const KeyT* src = kin + gs;
       KeyT* dst = reinterpret_cast<KeyT*>(dstk + (A - ck.a16));
       for (int i = 0; i < len; ++i) {
         const uint64_t addr = A + (uint64_t)i * sizeof(KeyT);
@@ -826,7 +900,7 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
       if constexpr (kHasVal) {
         if (carry) {
           unsigned char* dstv = stage_v + off_v;
-          const V* vsrc = a.vin + gs;
+          const V* vsrc = vin + gs;
           V* vdst = reinterpret_cast<V*>(dstv + (Av - cv.a16));
           for (int i = 0; i < len; ++i) {
             const uint64_t addr = Av + (uint64_t)i * sizeof(V);
@@ -852,6 +926,7 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
       d.meta[1] = gbase;
       d.meta[2] = g;
       d.meta[3] = any_bad ? -1 : total;
+      d.meta[4] = loc.flags;
       if (any_bad && a.err) atomicOr(a.err, DEV_BAD_SEGMENT);
     }
     // window table of every level: pair p of a level with `span` segments
@@ -1033,9 +1108,13 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
     if (t0 >= 0) {
       const KeyT* fk = (cur ? k1 : k0);
       const V* fv = (cur ? v1 : v0);
+      const int64_t tflags = d.meta[4];
+      KeyT* kout = (tflags & GRP_ALT) ? a.out2 : a.out;
+      V* vout = (tflags & GRP_ALT) ? a.vout2 : a.vout;
+      const int dec = a.dec_on_store | ((tflags & GRP_DEC) ? 1 : 0);
       for (int q = t0; q < cnt; q += nthr) {
-        a.out[out_base + q] = maybe_dec<Codec>(fk[q], a.dec_on_store);
-        if constexpr (kHasVal) a.vout[out_base + q] = fv[q];
+        kout[out_base + q] = maybe_dec<Codec>(fk[q], dec);
+        if constexpr (kHasVal) vout[out_base + q] = fv[q];
       }
       if (a.sample_out) {
         const int64_t rel0 = out_base - run_base;
@@ -1066,6 +1145,9 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
 // block of the run.  Between two boundaries every run contributes at most
 // (its blocks in that stretch of F + 1) blocks, so a tile holds at most
 // (G + K) * B keys.
+// Segmented rounds (grp set): row r belongs to group row_grp[r]; the group's
+// runs, block samples and merged sample follow its GroupDesc, and GRP_ALT
+// groups read `data2`.
 template <class KeyT, class Cmp, class Codec>
 __global__ void __launch_bounds__(256) splitter_kernel(const KeyT* __restrict__ data, const KeyT* __restrict__ samp,
                                                         const KeyT* __restrict__ fkeys,
@@ -1073,18 +1155,34 @@ __global__ void __launch_bounds__(256) splitter_kernel(const KeyT* __restrict__ 
                                                         int k, int64_t sample_run_len, int sample_b, int64_t G,
                                                         int64_t tiles_full, int64_t tiles_last, int64_t groups,
                                                         int64_t* __restrict__ desc, int64_t* __restrict__ doff,
-                                                        int enc) {
+                                                        int enc, const GroupDesc* __restrict__ grp,
+                                                        const int32_t* __restrict__ row_grp,
+                                                        const KeyT* __restrict__ data2) {
   const Cmp cmp;
   const int lane = threadIdx.x & 31;
   const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int64_t rows_per_group = tiles_full + 1;
-  const int64_t g = row / rows_per_group;
-  if (g >= groups) return;
-  const int64_t j = row - g * rows_per_group;
-  const int64_t jg = (g == groups - 1) ? tiles_last : tiles_full;
-  if (j > jg) return;
-  const int64_t gbase = g * L * k;
-  const int64_t ng = min64(L * k, n - gbase);
+  int64_t g, j, jg, gbase, ng, run0;
+  if (grp) {
+    if (row >= grp[groups].row0) return;
+    g = row_grp[row];
+    const GroupDesc& gd = grp[g];
+    j = row - gd.row0;
+    jg = grp[g + 1].tile0 - gd.tile0;
+    gbase = gd.start;
+    ng = gd.len;
+    run0 = gd.run0;
+    if (gd.flags & GRP_ALT) data = data2;
+  } else {
+    const int64_t rows_per_group = tiles_full + 1;
+    g = row / rows_per_group;
+    if (g >= groups) return;
+    j = row - g * rows_per_group;
+    jg = (g == groups - 1) ? tiles_last : tiles_full;
+    if (j > jg) return;
+    gbase = g * L * k;
+    ng = min64(L * k, n - gbase);
+    run0 = g * (int64_t)k;
+  }
   int64_t c = 0;
   if (lane < k) {
     const int64_t rs = min64((int64_t)lane * L, ng);
@@ -1095,11 +1193,11 @@ __global__ void __launch_bounds__(256) splitter_kernel(const KeyT* __restrict__ 
     } else if (j == jg) {
       c = len;
     } else {
-      const int64_t fpos = g * (int64_t)k * sample_run_len + j * G;
+      const int64_t fpos = run0 * sample_run_len + j * G;
       const KeyT v = fkeys[fpos];
       const int64_t sidx = (int64_t)fidx[fpos];
       const int64_t run = sidx / sample_run_len;
-      const int64_t kb = run - g * k;
+      const int64_t kb = run - run0;
       const int64_t ib = (sidx - run * sample_run_len) * sample_b;
       if (lane == kb) {
         c = ib;
@@ -1109,7 +1207,7 @@ __global__ void __launch_bounds__(256) splitter_kernel(const KeyT* __restrict__ 
         const bool le = lane < kb;
         auto precedes = [=](const KeyT& x) -> bool { return le ? !cmp(v, x) : cmp(x, v); };
         // 1. blocks whose first key precedes the boundary
-        const KeyT* sr = samp + (g * (int64_t)k + lane) * sample_run_len;
+        const KeyT* sr = samp + (run0 + lane) * sample_run_len;
         const int64_t nb = (len + sample_b - 1) / sample_b;
         int64_t lo = 0, hi = nb;
         while (lo < hi) {
@@ -1142,16 +1240,18 @@ __global__ void __launch_bounds__(256) splitter_kernel(const KeyT* __restrict__ 
 
 // ---------------------------------------------------------------------------
 // Block sample of a sample: out[r*out_run + b] = in[r*in_run + b*B] for every
-// run r and every b < ceil(len_r / B).
+// run r and every b < ceil(len_r / B).  Run lengths: in_run each, the last
+// one up to n_in; or, for segmented rounds, run_len[r].
 template <class KeyT, class Codec>
 __global__ void gather_sample_kernel(const KeyT* __restrict__ in, KeyT* __restrict__ out, int64_t n_in, int64_t in_run,
-                                     int64_t out_run, int b_step, int64_t n_out_slots, int enc) {
+                                     int64_t out_run, int b_step, int64_t n_out_slots, int enc,
+                                     const int32_t* __restrict__ run_len) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n_out_slots) return;
   const int64_t r = t / out_run;
   const int64_t b = t - r * out_run;
   const int64_t src = r * in_run + b * b_step;
-  const int64_t rend = min64((r + 1) * in_run, n_in);
+  const int64_t rend = run_len ? r * in_run + run_len[r] : min64((r + 1) * in_run, n_in);
   if (src < rend) out[t] = maybe_enc<Codec>(in[src], enc);
 }
 

@@ -6,9 +6,11 @@
 // Requests are device-resident key buffers (int32 keys, or uint64 keys with an
 // int32 payload); results go to caller-owned device output buffers; inputs are
 // never modified.  A dispatcher thread turns queued requests into work items:
-//   * int32 requests of at most `batch_max_keys` keys that are waiting
-//     together become ONE segmented sort (gms_segmented_sort_i32);
-//   * larger int32 requests and key/value requests run one per item.
+//   * requests of one kind of at most `batch_max_keys` keys that are waiting
+//     together become ONE batched sort (a segmented sort planned on the host
+//     from the requests' sizes, its plan uploaded from pinned memory, so the
+//     dispatcher never waits for a stream);
+//   * larger requests run one per item.
 // Each item is admitted only when its device memory (staging buffers,
 // allocated stream-ordered with cudaMallocAsync so no allocation stalls other
 // streams, plus the sort scratch of its stream) fits the memory budget still
@@ -21,13 +23,16 @@
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <algorithm>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <new>
 #include <thread>
 #include <vector>
 
 #include "gms_capi.cuh"
+#include "gms_capi_seg.cuh"
 
 using namespace gms_capi;
 
@@ -53,10 +58,17 @@ struct Item {
   std::vector<uint64_t> reqs;
   int stream_idx = 0;
   cudaEvent_t ev = nullptr;
-  size_t bytes = 0;              // budget charged
-  std::vector<void*> bufs;       // stream-ordered allocations to release
-  std::vector<int64_t> offsets;  // batch offsets (host source of an async copy)
+  size_t bytes = 0;         // budget charged
+  std::vector<void*> bufs;  // stream-ordered allocations to release
+  // batched items: the plan, its tuning, and the pinned slot its arrays are
+  // uploaded from (free again once the item's event completes)
+  std::unique_ptr<SegJob> job;
+  gms::Tune tune;
+  int pin_slot = -1;
 };
+
+// pinned upload slot of a batch plan
+constexpr size_t kPinSlotBytes = size_t(1) << 20;
 
 }  // namespace
 
@@ -87,6 +99,8 @@ struct gms_server {
   bool have_first = false;
 
   std::thread dispatcher, completer;
+  unsigned char* pin = nullptr;  // pinned slots of batch plans
+  std::vector<char> pin_free;
 };
 
 namespace {
@@ -94,16 +108,16 @@ namespace {
 size_t scratch_bytes_i32(int64_t n) { return gms_workspace_bytes(0, 0, n); }
 
 // Device memory one item needs beyond its stream's reserved scratch.
-size_t item_bytes(gms_server* s, const std::vector<uint64_t>& ids, bool batch) {
+size_t item_bytes(gms_server* s, const std::vector<uint64_t>& ids, bool batch, size_t plan_bytes) {
   int64_t n = 0;
   int kind = 0;
   for (uint64_t id : ids) {
     n += s->reqs[id].n;
     kind = s->reqs[id].kind;
   }
-  if (batch) return (size_t)n * (4 + 4) + (ids.size() + 1) * 8 + 4096;  // gathered in/out, offsets
-  if (kind == 0) return (size_t)n * 4 + 256;                                   // staging copy of the input
-  return (size_t)n * (8 + 4) + 512;                                            // staging keys + payload
+  const size_t elt = kind == 0 ? 4 : 8 + 4;
+  if (batch) return (size_t)n * elt * 2 + plan_bytes + 4096;  // gathered in/out, the plan
+  return (size_t)n * elt + 512;                               // staging copy of the input
 }
 
 void fail(gms_server* s, int status, const char* msg) {
@@ -125,25 +139,37 @@ int launch_item(gms_server* s, Item& it, const std::vector<Request*>& rs, bool b
     return p;
   };
   if (batch) {
-    std::vector<int64_t>& off = it.offsets;
-    off.assign(rs.size() + 1, 0);
+    const bool kvb = rs[0]->kind == 1;
+    const size_t kb = kvb ? sizeof(uint64_t) : sizeof(int32_t);
+    std::vector<int64_t> off(rs.size() + 1, 0);
     for (size_t i = 0; i < rs.size(); ++i) off[i + 1] = off[i] + rs[i]->n;
     const int64_t n = off.back();
-    int32_t* bin = (int32_t*)alloc(sizeof(int32_t) * n);
-    int32_t* bout = bin ? (int32_t*)alloc(sizeof(int32_t) * n) : nullptr;
-    int64_t* doff = bout ? (int64_t*)alloc(sizeof(int64_t) * off.size()) : nullptr;
-    if (!doff) return cuda_error(e, "cudaMallocAsync(batch)");
-    // the host offsets belong to the item, which lives until its event completes
-    e = cudaMemcpyAsync(doff, off.data(), sizeof(int64_t) * off.size(), cudaMemcpyHostToDevice, st);
-    if (e != cudaSuccess) return cuda_error(e, "offsets H2D");
+    SegJob* job = it.job.get();
+    unsigned char* bin = (unsigned char*)alloc(kb * n);
+    unsigned char* bout = bin ? (unsigned char*)alloc(kb * n) : nullptr;
+    int32_t* vbin = (bout && kvb) ? (int32_t*)alloc(sizeof(int32_t) * n) : nullptr;
+    int32_t* vbout = vbin ? (int32_t*)alloc(sizeof(int32_t) * n) : nullptr;
+    void* dblob = (bout && (!kvb || vbout)) ? alloc(job->blob.bytes) : nullptr;
+    if (!dblob) return cuda_error(e, "cudaMallocAsync(batch)");
+    // the plan's arrays, from the item's pinned slot (an asynchronous copy)
+    unsigned char* slot = s->pin + (size_t)it.pin_slot * kPinSlotBytes;
+    gms::seg_blob_fill(job->plan, job->blob, slot);
+    e = cudaMemcpyAsync(dblob, slot, job->blob.bytes, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_error(e, "plan H2D");
     for (size_t i = 0; i < rs.size(); ++i) {
-      e = cudaMemcpyAsync(bin + off[i], rs[i]->kin, sizeof(int32_t) * rs[i]->n, cudaMemcpyDeviceToDevice, st);
+      e = cudaMemcpyAsync(bin + kb * off[i], rs[i]->kin, kb * rs[i]->n, cudaMemcpyDeviceToDevice, st);
+      if (e == cudaSuccess && kvb)
+        e = cudaMemcpyAsync(vbin + off[i], rs[i]->vin, sizeof(int32_t) * rs[i]->n, cudaMemcpyDeviceToDevice, st);
       if (e != cudaSuccess) return cuda_error(e, "gather D2D");
     }
-    int status = gms_segmented_sort_i32(bin, bout, n, doff, (int64_t)rs.size(), st);
+    const int status = kvb ? seg_run_kv_u64(job, dblob, (const uint64_t*)bin, vbin, (uint64_t*)bout, vbout, n,
+                                            it.tune, st)
+                           : seg_run_i32(job, dblob, (const int32_t*)bin, (int32_t*)bout, n, it.tune, st);
     if (status != GMS_OK) return status;
     for (size_t i = 0; i < rs.size(); ++i) {
-      e = cudaMemcpyAsync(rs[i]->kout, bout + off[i], sizeof(int32_t) * rs[i]->n, cudaMemcpyDeviceToDevice, st);
+      e = cudaMemcpyAsync(rs[i]->kout, bout + kb * off[i], kb * rs[i]->n, cudaMemcpyDeviceToDevice, st);
+      if (e == cudaSuccess && kvb)
+        e = cudaMemcpyAsync(rs[i]->vout, vbout + off[i], sizeof(int32_t) * rs[i]->n, cudaMemcpyDeviceToDevice, st);
       if (e != cudaSuccess) return cuda_error(e, "scatter D2D");
     }
   } else {
@@ -184,12 +210,13 @@ void dispatcher_main(gms_server* s) {
     bool batch = false;
     const uint64_t head = s->queue.front();
     const Request& h = s->reqs[head];
-    if (h.kind == 0 && h.n <= s->batch_max_keys) {
-      // every small int32 request waiting now joins the batch (up to the cap)
+    if (h.n <= s->batch_max_keys) {
+      // every small request of the head's kind waiting now joins the batch (up
+      // to the cap)
       int64_t tot = 0;
       for (auto it = s->queue.begin(); it != s->queue.end();) {
         const Request& r = s->reqs[*it];
-        if (r.kind == 0 && r.n <= s->batch_max_keys && tot + r.n <= s->batch_cap_keys) {
+        if (r.kind == h.kind && r.n <= s->batch_max_keys && tot + r.n <= s->batch_cap_keys) {
           ids.push_back(*it);
           tot += r.n;
           it = s->queue.erase(it);
@@ -204,7 +231,31 @@ void dispatcher_main(gms_server* s) {
     }
     Item it;
     it.reqs = ids;
-    it.bytes = item_bytes(s, ids, batch);
+    size_t plan_bytes = 0;
+    if (batch) {
+      // plan the batch from its sizes, here on the host
+      std::vector<int64_t> off(ids.size() + 1, 0);
+      for (size_t i = 0; i < ids.size(); ++i) off[i + 1] = off[i] + s->reqs[ids[i]].n;
+      const int kind = s->reqs[ids[0]].kind;
+      it.tune = tune_for(kind == 0 ? 0 : 4, kind, off.back());
+      it.job.reset(new (std::nothrow) SegJob);
+      int st2 = it.job ? (kind == 0 ? seg_prepare_i32(off, (int64_t)ids.size(), it.tune, it.job.get())
+                                    : seg_prepare_kv_u64(off, (int64_t)ids.size(), it.tune, it.job.get()))
+                       : GMS_ERR_NOMEM;
+      if (st2 == GMS_OK && it.job->blob.bytes > kPinSlotBytes) st2 = GMS_ERR_TOO_LARGE;
+      if (st2 != GMS_OK) {
+        for (uint64_t id : ids) {
+          Request& r = s->reqs[id];
+          r.status = st2;
+          r.done = true;
+          r.t_done = Clock::now();
+        }
+        s->cv_done.notify_all();
+        continue;
+      }
+      plan_bytes = it.job->blob.bytes;
+    }
+    it.bytes = item_bytes(s, ids, batch, plan_bytes);
     // admission: wait until the item fits the budget that is still free
     if (it.bytes > s->budget) {
       for (uint64_t id : ids) {
@@ -217,6 +268,18 @@ void dispatcher_main(gms_server* s) {
       continue;
     }
     s->cv_budget.wait(lk, [&] { return s->stop || s->in_use + it.bytes <= s->budget; });
+    if (batch) {
+      // a free pinned slot for the plan upload (freed by the completer)
+      auto free_slot = [&] {
+        for (size_t i = 0; i < s->pin_free.size(); ++i)
+          if (s->pin_free[i]) return (int)i;
+        return -1;
+      };
+      s->cv_budget.wait(lk, [&] { return s->stop || free_slot() >= 0; });
+      it.pin_slot = free_slot();
+      if (it.pin_slot < 0) it.pin_slot = 0;  // stopping: the item still runs to completion
+      s->pin_free[(size_t)it.pin_slot] = 0;
+    }
     s->in_use += it.bytes;
     it.stream_idx = s->next_stream;
     s->next_stream = (s->next_stream + 1) % (int)s->streams.size();
@@ -259,6 +322,7 @@ void completer_main(gms_server* s) {
     lk.lock();
     if (e != cudaSuccess) fail(s, cuda_error(e, "item event"), gms_last_error());
     s->in_use -= it.bytes;
+    if (it.pin_slot >= 0) s->pin_free[(size_t)it.pin_slot] = 1;
     for (uint64_t id : it.reqs) {
       Request& r = s->reqs[id];
       r.done = true;
@@ -309,16 +373,32 @@ int gms_server_create(size_t memory_budget, int nstreams, int64_t batch_max_keys
       return cuda_error(e, "cudaStreamCreate");
     }
     s->streams.push_back(st);
-    // scratch of every stream sized once for the largest request, so no sort
-    // allocates while the server runs
-    int status = gms_reserve(0, 0, max_request_keys > s->batch_cap_keys ? max_request_keys : s->batch_cap_keys, st);
-    if (status == GMS_OK) status = gms_reserve(4, 1, max_request_keys, st);
-    if (status == GMS_OK) status = gms_reserve(GMS_RESERVE_SEGMENTED_I32, 0, s->batch_cap_keys, st);
+    // scratch of every stream sized once for the largest request or batch,
+    // so no sort allocates while the server runs: the plain sorts' scratch
+    // (with room for a batch plan's somewhat larger sample arrays) and the
+    // batched sorts' scratch arrays of keys and payload
+    const int64_t most = max_request_keys > s->batch_cap_keys ? max_request_keys : s->batch_cap_keys;
+    const size_t ws = std::max(gms_workspace_bytes(0, 0, most), gms_workspace_bytes(4, 1, most));
+    int status = GMS_OK;
+    cache_get(0, ws + ws / 4 + (size_t(1) << 20), st, &status);
+    if (status == GMS_OK) cache_get(30, sizeof(uint64_t) * (size_t)s->batch_cap_keys, st, &status);
+    if (status == GMS_OK) cache_get(31, sizeof(int32_t) * (size_t)s->batch_cap_keys, st, &status);
     if (status != GMS_OK) {
       for (cudaStream_t x : s->streams) cudaStreamDestroy(x);
       delete s;
       return status;
     }
+  }
+  // pinned upload slots of batch plans, two per stream
+  {
+    const size_t nslots = 2 * s->streams.size();
+    cudaError_t e = cudaMallocHost((void**)&s->pin, nslots * kPinSlotBytes);
+    if (e != cudaSuccess) {
+      for (cudaStream_t x : s->streams) cudaStreamDestroy(x);
+      delete s;
+      return cuda_error(e, "cudaMallocHost(plan slots)");
+    }
+    s->pin_free.assign(nslots, 1);
   }
   // keep freed stream-ordered staging memory mapped up to the budget
   cudaMemPool_t pool;
@@ -430,6 +510,7 @@ int gms_server_destroy(gms_server* s) {
     cudaStreamSynchronize(st);
     cudaStreamDestroy(st);
   }
+  cudaFreeHost(s->pin);
   delete s;
   return GMS_OK;
 }

@@ -28,6 +28,7 @@
 
 #include "gms_host_plan.h"
 #include "gms_kernels.cuh"
+#include "gms_seg_plan.h"
 
 namespace gms {
 
@@ -266,6 +267,65 @@ struct RoundSplit {
   void* ctx = nullptr;
 };
 
+// Device view of one round of a segmented plan (gms_seg_plan.h): its listed
+// groups and maps, and the round of its sample merges.
+struct SegLevelDev {
+  int64_t n = 0, L = 0, runs = 0, groups = 0, tiles = 0, rows = 0;
+  bool whole = false;
+  const GroupDesc* grp = nullptr;
+  const int32_t* tile_grp = nullptr;
+  const int32_t* row_grp = nullptr;
+  const int32_t* run_len = nullptr;
+  const SegLevelDev* sample = nullptr;
+};
+struct SegDev {
+  const GroupDesc* base = nullptr;
+  int64_t base_tiles = 0;
+  std::vector<SegLevelDev> levels;
+  std::vector<int> rounds;  // level of data rounds 1 .. R
+};
+
+// Binds a plan's levels to its arrays uploaded at `blob` (seg_blob_layout).
+inline void seg_bind(const SegPlanH& P, const SegBlob& b, const void* blob, SegDev* D) {
+  const unsigned char* c = static_cast<const unsigned char*>(blob);
+  D->base = reinterpret_cast<const GroupDesc*>(c + b.base);
+  D->base_tiles = (int64_t)P.base.size();
+  D->levels.assign(P.levels.size(), SegLevelDev{});
+  for (size_t i = 0; i < P.levels.size(); ++i) {
+    const SegLevelH& l = P.levels[i];
+    SegLevelDev& d = D->levels[i];
+    d.n = l.n;
+    d.L = l.L;
+    d.runs = l.runs;
+    d.groups = (int64_t)l.grp.size() - 1;
+    d.tiles = (int64_t)l.tile_grp.size();
+    d.rows = (int64_t)l.row_grp.size();
+    d.whole = l.whole;
+    d.grp = reinterpret_cast<const GroupDesc*>(c + b.lv[i].grp);
+    d.tile_grp = reinterpret_cast<const int32_t*>(c + b.lv[i].tile_grp);
+    d.row_grp = reinterpret_cast<const int32_t*>(c + b.lv[i].row_grp);
+    d.run_len = reinterpret_cast<const int32_t*>(c + b.lv[i].run_len);
+  }
+  for (size_t i = 0; i < P.levels.size(); ++i) {
+    if (P.levels[i].sample >= 0) D->levels[i].sample = &D->levels[(size_t)P.levels[i].sample];
+  }
+  D->rounds = P.rounds;
+}
+
+// Scratch layout of a segmented plan (same parts as a plain sort's).
+inline WsLayout seg_ws_layout(const SegPlanH& P) {
+  WsLayout l;
+  l.s1 = P.s1;
+  for (int i = 0; i < kMaxLevels && i < 8; ++i) {
+    l.s[i] = P.s[i];
+    l.f[i] = P.f[i];
+    l.rows[i] = P.rows[i];
+  }
+  l.depth = P.depth;
+  l.ok = P.ok;
+  return l;
+}
+
 // Geometry of the merge kernels of one payload type: NT threads x ITEMS keys,
 // NS merge streams per thread.  CAP bounds a group merged by one CTA
 // (tile_kernel), CAPW a forecast tile (merge_tiles_kernel, window-aligned).
@@ -448,13 +508,26 @@ struct Engine {
   // One K-way round over runs of length L.  `sample_in` is the block sample of
   // `in` (null: gather it here); `sample_out` receives the block sample of the
   // output runs (null: not needed).
+  // Segmented rounds (sl set): the groups are listed by the plan level `sl`,
+  // groups flagged GRP_ALT read in2/vin2 and write out2/vout2, and the round
+  // never uses the plain-load tile path (staging mode 0 runs as mode 1).
   template <class VV>
   static cudaError_t round(const WsPtrs<KeyT>& w, int level, const KeyT* in, const VV* vin, KeyT* out, VV* vout, int64_t n,
                            int64_t L, const Tune& t, const KeyT* sample_in, KeyT* sample_out, int enc, int dec,
-                           int gen_index, cudaStream_t st, const RoundSplit* split = nullptr) {
+                           int gen_index, cudaStream_t st, const RoundSplit* split = nullptr,
+                           const SegLevelDev* sl = nullptr, const KeyT* in2 = nullptr, KeyT* out2 = nullptr,
+                           const VV* vin2 = nullptr, VV* vout2 = nullptr) {
     const int k = t.k;
     const int sb = t.sample_b;
     TileArgs<KeyT, VV> a{};
+    if (sl) {
+      a.grp = sl->grp;
+      a.tile_grp = sl->tile_grp;
+      a.in2 = in2;
+      a.out2 = out2;
+      a.vin2 = vin2;
+      a.vout2 = vout2;
+    }
     a.in = in;
     a.out = out;
     a.vin = vin;
@@ -470,22 +543,25 @@ struct Engine {
     a.sample_b = sb;
     a.out_run_len = L * k;
     a.sample_run_len = ceil_div(L * k, sb);
-    const int64_t groups = ceil_div(n, L * k);
+    const int64_t groups = sl ? sl->groups : ceil_div(n, L * k);
+    a.groups = groups;
     if ((int64_t)k * L <= Geo<VV>::CAP) {
       return launch_tile<MODE_GROUP>(a, groups, st, level);
     }
     if (level + 1 >= kMaxLevels) return cudaErrorInvalidValue;
     const int64_t G = Geo<VV>::CAPW / sb - k;
-    const int64_t runs = ceil_div(n, L);
+    const int64_t runs = sl ? sl->runs : ceil_div(n, L);
     const int64_t Ls = ceil_div(L, sb);
-    const int64_t ns = (runs - 1) * Ls + ceil_div(n - (runs - 1) * L, sb);
+    // listed groups keep every run's block sample Ls apart (gaps after short runs)
+    const int64_t ns = sl ? runs * Ls : (runs - 1) * Ls + ceil_div(n - (runs - 1) * L, sb);
     cudaError_t e;
     const KeyT* S = sample_in;
     if (!S) {
       KeyT* g = w.s[level + 1];
       const int64_t slots = runs * Ls;
       hook_before(KC_GATHER, st);
-      gather_sample_kernel<KeyT, Codec><<<(unsigned)ceil_div(slots, 256), 256, 0, st>>>(in, g, n, L, Ls, sb, slots, enc);
+      gather_sample_kernel<KeyT, Codec><<<(unsigned)ceil_div(slots, 256), 256, 0, st>>>(
+          in, g, n, L, Ls, sb, slots, enc, sl ? sl->run_len : nullptr);
       e = cudaGetLastError();
       hook_after(KC_GATHER, st);
       if (e != cudaSuccess) return e;
@@ -493,19 +569,19 @@ struct Engine {
     }
     // 1. merge the block samples of each group, keeping each sample's index
     e = round<IdxT>(w, level + 1, S, nullptr, w.fk[level + 1], w.fi[level + 1], ns, Ls, t, nullptr, nullptr, 0, 0, 1,
-                    st);
+                    st, nullptr, sl ? sl->sample : nullptr);
     if (e != cudaSuccess) return e;
     // 2. tile boundaries
     const int64_t tiles_full = ceil_div((int64_t)k * Ls, G);
     const int64_t last_ns = ns - (groups - 1) * (int64_t)k * Ls;
     const int64_t tiles_last = ceil_div(last_ns, G);
-    const int64_t rows = groups * (tiles_full + 1);
+    const int64_t rows = sl ? sl->rows : groups * (tiles_full + 1);
     {
       const int64_t threads = rows * 32;
       hook_before(KC_SPLIT, st);
       splitter_kernel<KeyT, Cmp, Codec><<<(unsigned)ceil_div(threads, 256), 256, 0, st>>>(
           in, S, w.fk[level + 1], w.fi[level + 1], n, L, k, Ls, sb, G, tiles_full, tiles_last, groups, w.desc[level],
-          w.doff[level], enc);
+          w.doff[level], enc, sl ? sl->grp : nullptr, sl ? sl->row_grp : nullptr, in2);
       e = cudaGetLastError();
       hook_after(KC_SPLIT, st);
       if (e != cudaSuccess) return e;
@@ -515,7 +591,7 @@ struct Engine {
     a.doff = w.doff[level];
     a.tiles_full = tiles_full;
     a.tiles_last = tiles_last;
-    a.groups = groups;
+    if (sl) return launch_merge_tiles(a, sl->tiles, st, level, t.bulk_copy ? t.bulk_copy : 1);
     if (t.bulk_copy && split && split->parts > 1 && groups == 1 && tiles_last > 1) {
       int64_t ends[kMaxParts];
       const int np = host_split_ends(tiles_last, split->parts, split->ramp, ends);
@@ -665,6 +741,69 @@ struct Engine {
       cur ^= 1;
       sbuf ^= 1;
       L *= t.k;
+    }
+    return cudaSuccess;
+  }
+
+  // ---------------- segmented sorts ----------------
+  static SegGeom seg_geom(const Tune& t) {
+    SegGeom g;
+    g.base_tile = BASE_TILE;
+    g.cap_data = Geo<V>::CAP;
+    g.capw_data = Geo<V>::CAPW;
+    g.cap_idx = Geo<IdxT>::CAP;
+    g.capw_idx = Geo<IdxT>::CAPW;
+    g.k = t.k;
+    g.sample_b = t.sample_b;
+    g.max_levels = kMaxLevels;
+    return g;
+  }
+
+  // Sorts every segment of a plan bound as D: `src` (n keys, with payload
+  // `vsrc`) is read only, `tmp` is scratch of n keys (+ payload), the sorted
+  // segments land in `dst`.  One base-case launch over every segment's tiles,
+  // then one launch sequence per round over the groups of the segments that
+  // still need it; each segment's last round (or its base case) writes `dst`.
+  static cudaError_t seg_sort(const WsPtrs<KeyT>& w, const SegDev& D, const KeyT* src, const V* vsrc, KeyT* tmp,
+                              V* vtmp, KeyT* dst, V* vdst, int64_t n, const Tune& t0, cudaStream_t st) {
+    if (n <= 0 || D.base_tiles == 0) return cudaSuccess;
+    Tune t = t0;
+    if (t.bulk_copy == 0) t.bulk_copy = 1;
+    const int R = (int)D.rounds.size();
+    TileArgs<KeyT, V> a{};
+    a.in = src;
+    a.out = tmp;
+    a.vin = vsrc;
+    a.vout = vtmp;
+    a.in2 = src;
+    a.out2 = dst;
+    a.vin2 = vsrc;
+    a.vout2 = vdst;
+    a.n = n;
+    a.L = BASE_TILE;
+    a.k = 1;
+    a.enc_on_load = 1;
+    a.dec_on_store = 0;
+    a.err = w.err;
+    a.grp = D.base;
+    a.sample_b = t.sample_b;
+    a.out_run_len = BASE_TILE;
+    a.sample_run_len = ceil_div(BASE_TILE, t.sample_b);
+    a.sample_out = R > 0 ? w.s1[0] : nullptr;
+    cudaError_t e;
+    if constexpr (kWarpBase) {
+      e = launch_base_warp(a, D.base_tiles, st);
+    } else {
+      e = launch_tile<MODE_BASE>(a, D.base_tiles, st);
+    }
+    if (e != cudaSuccess) return e;
+    int64_t L = BASE_TILE;
+    for (int p = 0; p < R; ++p, L *= t.k) {
+      const SegLevelDev* sl = &D.levels[(size_t)D.rounds[(size_t)p]];
+      KeyT* sout = (p + 1 < R) ? w.s1[(p + 1) & 1] : nullptr;
+      e = round<V>(w, 0, tmp, vtmp, dst, vdst, n, L, t, w.s1[p & 1], sout, 0, 0, 0, st, nullptr, sl, dst, tmp, vdst,
+                   vtmp);
+      if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
   }

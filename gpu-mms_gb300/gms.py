@@ -161,6 +161,15 @@ SIGNATURES = {
     "gms_segmented_sort_i32": (_i32, [_vp, _vp, _i64, _vp, _i64, _vp]),
     "gms_segmented_sort_u32": (_i32, [_vp, _vp, _i64, _vp, _i64, _vp]),
     "gms_segmented_sort_f32": (_i32, [_vp, _vp, _i64, _vp, _i64, _vp]),
+    "gms_segmented_sort_i64": (_i32, [_vp, _vp, _i64, _vp, _i64, _vp]),
+    "gms_segmented_sort_u64": (_i32, [_vp, _vp, _i64, _vp, _i64, _vp]),
+    "gms_segmented_sort_f64": (_i32, [_vp, _vp, _i64, _vp, _i64, _vp]),
+    "gms_segmented_sort_kv_i32_i32": (_i32, [_vp, _vp, _vp, _vp, _i64, _vp, _i64, _vp]),
+    "gms_segmented_sort_kv_u32_i32": (_i32, [_vp, _vp, _vp, _vp, _i64, _vp, _i64, _vp]),
+    "gms_segmented_sort_kv_f32_i32": (_i32, [_vp, _vp, _vp, _vp, _i64, _vp, _i64, _vp]),
+    "gms_segmented_sort_kv_i64_i32": (_i32, [_vp, _vp, _vp, _vp, _i64, _vp, _i64, _vp]),
+    "gms_segmented_sort_kv_u64_i32": (_i32, [_vp, _vp, _vp, _vp, _i64, _vp, _i64, _vp]),
+    "gms_segmented_sort_kv_f64_i32": (_i32, [_vp, _vp, _vp, _vp, _i64, _vp, _i64, _vp]),
     "gms_graph_create_sort_i32": (_i32, [_vp, _vp, _i64, _vp, ctypes.POINTER(_vp)]),
     "gms_graph_create_segmented_i32": (_i32, [_vp, _vp, _i64, _vp, _i64, _vp, ctypes.POINTER(_vp)]),
     "gms_graph_launch": (_i32, [_vp, _vp]),

@@ -189,20 +189,47 @@ int gms_find_partitions_i32(const int32_t* task, int64_t size, int k, int64_t ta
  * Batched (segmented) sorts: `n` keys forming `nseg` independent arrays;
  * array s is [offsets[s], offsets[s+1]) with offsets[0] = 0 and
  * offsets[nseg] = n (device int64, nseg+1 entries; empty arrays allowed).
- * Every array is sorted into the same range of `output`; `input` is not
- * modified.  One sort of 64-bit (array, key) composites sorts them all: every
- * round is one launch over all arrays.  Bad offsets set bit 3 (value 8) of the
- * device status word (gms_device_status).
+ * Every array is sorted into the same range of `output` (payload sorts:
+ * stably, with the payload); the inputs are not modified.
+ *
+ * Each array gets its own base-case tiles and merge rounds -- no group of a
+ * round crosses an array's end -- and every round is one launch sequence
+ * over all the arrays that still need it: an array of at most one base tile
+ * (gms_base_tile) is sorted in a single pass, one of up to 32 tiles in one
+ * merge round, larger ones in rounds bounded to the array.  The call reads
+ * the offsets back to plan the batch (it waits for `stream` to reach them),
+ * then enqueues the sort asynchronously.  Offsets that do not rise from 0 to
+ * n are GMS_ERR_INVALID.  Scratch: about n keys (+ payload) beyond a plain
+ * sort's, from the per-stream cache.
  *
  * No counterpart in the reference: GPU-MMS sorts one array per
- * multimergesort call (src/multimergesort.hxx:56-141).
+ * multimergesort call (src/multimergesort.hxx:56-141), each running the
+ * round loop of multimergesort.hxx:87-135 on its own.
  * ------------------------------------------------------------------------- */
-int gms_segmented_sort_i32(int32_t* input, int32_t* output, int64_t n, const int64_t* offsets, int64_t nseg,
+int gms_segmented_sort_i32(const int32_t* input, int32_t* output, int64_t n, const int64_t* offsets, int64_t nseg,
                            void* stream);
-int gms_segmented_sort_u32(uint32_t* input, uint32_t* output, int64_t n, const int64_t* offsets, int64_t nseg,
+int gms_segmented_sort_u32(const uint32_t* input, uint32_t* output, int64_t n, const int64_t* offsets, int64_t nseg,
                            void* stream);
-int gms_segmented_sort_f32(float* input, float* output, int64_t n, const int64_t* offsets, int64_t nseg,
+int gms_segmented_sort_f32(const float* input, float* output, int64_t n, const int64_t* offsets, int64_t nseg,
                            void* stream);
+int gms_segmented_sort_i64(const int64_t* input, int64_t* output, int64_t n, const int64_t* offsets, int64_t nseg,
+                           void* stream);
+int gms_segmented_sort_u64(const uint64_t* input, uint64_t* output, int64_t n, const int64_t* offsets, int64_t nseg,
+                           void* stream);
+int gms_segmented_sort_f64(const double* input, double* output, int64_t n, const int64_t* offsets, int64_t nseg,
+                           void* stream);
+int gms_segmented_sort_kv_i32_i32(const int32_t* keys_in, const int32_t* vals_in, int32_t* keys_out, int32_t* vals_out,
+                                  int64_t n, const int64_t* offsets, int64_t nseg, void* stream);
+int gms_segmented_sort_kv_u32_i32(const uint32_t* keys_in, const int32_t* vals_in, uint32_t* keys_out,
+                                  int32_t* vals_out, int64_t n, const int64_t* offsets, int64_t nseg, void* stream);
+int gms_segmented_sort_kv_f32_i32(const float* keys_in, const int32_t* vals_in, float* keys_out, int32_t* vals_out,
+                                  int64_t n, const int64_t* offsets, int64_t nseg, void* stream);
+int gms_segmented_sort_kv_i64_i32(const int64_t* keys_in, const int32_t* vals_in, int64_t* keys_out, int32_t* vals_out,
+                                  int64_t n, const int64_t* offsets, int64_t nseg, void* stream);
+int gms_segmented_sort_kv_u64_i32(const uint64_t* keys_in, const int32_t* vals_in, uint64_t* keys_out,
+                                  int32_t* vals_out, int64_t n, const int64_t* offsets, int64_t nseg, void* stream);
+int gms_segmented_sort_kv_f64_i32(const double* keys_in, const int32_t* vals_in, double* keys_out, int32_t* vals_out,
+                                  int64_t n, const int64_t* offsets, int64_t nseg, void* stream);
 
 /* ---------------------------------------------------------------------------
  * CUDA graphs: capture the whole launch sequence of one sort (fixed pointers
@@ -210,7 +237,9 @@ int gms_segmented_sort_f32(float* input, float* output, int64_t n, const int64_t
  * sort once outside capture (setting kernel attributes and sizing scratch;
  * `input` is clobbered as by any sort), then captures it on `stream` (which
  * must not be the legacy default stream).  Replaying re-sorts whatever
- * `input` then holds into `output`.
+ * `input` then holds into `output`.  A batched graph plans the batch from
+ * the offsets at creation (the offsets must not change afterwards) and owns
+ * its scratch, which gms_graph_destroy frees.
  * No counterpart in the reference (it launches every kernel from the host
  * loop, src/multimergesort.hxx:87-135).
  * ------------------------------------------------------------------------- */
@@ -230,9 +259,9 @@ int gms_graph_destroy(gms_graph* graph);
  * device with `nstreams` streams.  Requests (gms_server_submit) are device
  * buffers: kind 0 = int32 keys, kind 1 = uint64 keys + int32 payload (stable);
  * inputs are never modified; results go to the caller's output buffers.
- * int32 requests of at most `batch_max_keys` keys that wait together are
- * sorted as ONE batched sort; larger and key/value requests run one per work
- * item.  A work item starts only when its staging memory (stream-ordered
+ * Requests of one kind of at most `batch_max_keys` keys that wait together
+ * are sorted as ONE batched sort (planned on the host, its plan uploaded from
+ * pinned memory); larger requests run one per work item.  A work item starts only when its staging memory (stream-ordered
  * cudaMallocAsync) fits what is left of `memory_budget`; items run on the
  * stream pool concurrently while new requests keep arriving.  Each stream's
  * sort scratch is reserved at creation for `max_request_keys` keys (outside
@@ -258,7 +287,8 @@ int gms_server_destroy(gms_server* server);
  * ------------------------------------------------------------------------- */
 /* dtype codes: 0=i32 1=u32 2=f32 3=i64 4=u64 5=f64; kv: 1 = with int32 payload.
  * gms_reserve also accepts GMS_RESERVE_SEGMENTED_I32 (batched 32-bit sorts of
- * up to n keys in all). */
+ * up to n keys in all: the scratch array of n keys and a plain sort's scratch;
+ * batches of many short arrays can need somewhat more). */
 #define GMS_RESERVE_SEGMENTED_I32 6
 size_t gms_workspace_bytes(int dtype, int kv, int64_t n);
 int gms_reserve(int dtype, int kv, int64_t n, void* stream);

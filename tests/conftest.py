@@ -92,6 +92,22 @@ class Oracle:
         getattr(self.lib, fn)(ptr(k), ptr(v), k.size)
         return k, v
 
+    def segmented_sort(self, a, off):
+        """Every [off[s], off[s+1]) sorted on its own (int32 or uint64 keys)."""
+        a = np.ascontiguousarray(a).copy()
+        off = np.ascontiguousarray(off, dtype=np.int64)
+        fn = {np.dtype(np.int32): "gmo_segmented_sort_i32", np.dtype(np.uint64): "gmo_segmented_sort_u64"}[a.dtype]
+        getattr(self.lib, fn)(ptr(a), ptr(off), len(off) - 1)
+        return a
+
+    def segmented_sort_kv_u64(self, k, v, off):
+        """Every [off[s], off[s+1]) sorted stably by its uint64 keys, int32 payload along."""
+        k = np.ascontiguousarray(k, dtype=np.uint64).copy()
+        v = np.ascontiguousarray(v, dtype=np.int32).copy()
+        off = np.ascontiguousarray(off, dtype=np.int64)
+        self.lib.gmo_segmented_sort_kv_u64_i32(ptr(k), ptr(v), ptr(off), len(off) - 1)
+        return k, v
+
     def tile_sort(self, a, tile):
         a = np.ascontiguousarray(a).copy()
         fn = self.lib.gmo_tile_sort_i32 if a.dtype == np.int32 else self.lib.gmo_tile_sort_u64
