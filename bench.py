@@ -587,6 +587,65 @@ def summarize(d):
     return out
 
 
+def profile_run(lib, orc, args):
+    """Warm-up + 1 calls of one workload and nothing else, for ncu captures of
+    the kernels it launches: int32 / u64 keys-only sorts, u64 / float32 keys
+    with an int32 payload, a batched int32 sort (arrays log-uniform in [32,
+    2^20] up to --n keys), or co-ranks of 32 runs at 8192 ranks."""
+    import numpy as np
+    import torch
+
+    n = args.n
+    sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    if args.bulk_copy is not None:
+        assert lib.gms_set_tune(32, 32, args.bulk_copy) == 0, lib.gms_last_error()
+    calls = args.warmup + 1
+    if args.what in ("int32", "u64"):
+        src = torch.from_numpy(orc.gen_i32(n, 0, SEED) if args.what == "int32"
+                               else orc.gen_u64(n, SEED).view(np.int64)).cuda()
+        fn = lib.gms_sort_i32 if args.what == "int32" else lib.gms_sort_u64
+        tin, tout = torch.empty_like(src), torch.empty_like(src)
+        for _ in range(calls):
+            tin.copy_(src)
+            assert fn(tin.data_ptr(), tout.data_ptr(), n, 0, sp) == 0, lib.gms_last_error()
+    elif args.what in ("kv_u64", "kv_f32"):
+        keys = orc.gen_u64(n, SEED).view(np.int64) if args.what == "kv_u64" else orc.gen_f32(n, SEED).view(np.int32)
+        src = torch.from_numpy(keys).cuda()
+        vals = torch.arange(n, dtype=torch.int32, device="cuda")
+        fn = lib.gms_sort_kv_u64_i32 if args.what == "kv_u64" else lib.gms_sort_kv_f32_i32
+        ki, vi = torch.empty_like(src), torch.empty_like(vals)
+        ko, vo = torch.empty_like(src), torch.empty_like(vals)
+        for _ in range(calls):
+            ki.copy_(src)
+            vi.copy_(vals)
+            assert fn(ki.data_ptr(), vi.data_ptr(), ko.data_ptr(), vo.data_ptr(), n, 0, sp) == 0, lib.gms_last_error()
+    elif args.what == "batched":
+        rng = np.random.default_rng(7)
+        lengths = log_uniform_lengths(rng, 32, 1 << 20, total_cap=n)
+        off = np.zeros(len(lengths) + 1, dtype=np.int64)
+        np.cumsum(lengths, out=off[1:])
+        n = int(off[-1])
+        src = torch.from_numpy(orc.gen_i32(n, 0, SEED)).cuda()
+        toff = torch.from_numpy(off).cuda()
+        out = torch.empty_like(src)
+        for _ in range(calls):
+            assert lib.gms_segmented_sort_i32(src.data_ptr(), out.data_ptr(), n, toff.data_ptr(), len(lengths),
+                                              sp) == 0, lib.gms_last_error()
+    else:
+        # co-ranks: 32 sorted runs of n/32 keys, 8192 equal-share ranks
+        size = max(1, n // 32)
+        runs = np.sort(orc.gen_i32(size * 32, 0, SEED).reshape(32, size), axis=1).reshape(-1)
+        task = torch.from_numpy(runs).cuda()
+        ranks = torch.linspace(0, size * 32, 8192, dtype=torch.float64).to(torch.int64).cuda()
+        outc = torch.empty((8192, 32), dtype=torch.int64, device="cuda")
+        for _ in range(calls):
+            assert lib.gms_find_partitions_i32(task.data_ptr(), size, 32, size * 32, ranks.data_ptr(), 8192,
+                                               outc.data_ptr(), sp) == 0, lib.gms_last_error()
+    torch.cuda.synchronize()
+    print(json.dumps({"mode": "profile", "what": args.what, "n": n, "calls": calls}), flush=True)
+    return 0
+
+
 def run_reference(args):
     """CPU arm: the oracle's std::sort with every host thread."""
     import numpy as np
@@ -868,6 +927,11 @@ def main():
                          "profile: warm-up sorts plus one sort of --n keys and nothing else (for ncu); "
                          "trace: the timeline of one synchronous host-to-host sort of --n keys")
     ap.add_argument("--trace-out", default=None, help="trace mode: also write every launch and copy as CSV here")
+    ap.add_argument("--what", default="int32", choices=["int32", "u64", "kv_u64", "kv_f32", "batched", "corank"],
+                    help="profile mode: the workload (each runs warm-up + 1 calls of --n keys and nothing else)")
+    ap.add_argument("--bulk-copy", type=int, default=None,
+                    help="profile mode: staging mode of the merge rounds (0 plain loads, 1 bulk copies, 2 cp.async, "
+                         "3 persistent); default: the library's choice")
     ap.add_argument("--rate", type=float, default=2000.0, help="serve mode: arrivals per second (0: all at once)")
     ap.add_argument("--max-size", type=int, default=1 << 26, help="serve mode: largest request (keys)")
     ap.add_argument("--seconds", type=float, default=60.0, help="serve mode: arrival window")
@@ -886,16 +950,7 @@ def main():
         lib = gms.load()
         orc = Oracle()
         if args.mode == "profile":
-            n = args.n
-            src = torch.from_numpy(orc.gen_i32(n, 0, SEED)).cuda()
-            tin, tout = torch.empty_like(src), torch.empty_like(src)
-            sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
-            for _ in range(args.warmup + 1):
-                tin.copy_(src)
-                assert lib.gms_sort_i32(tin.data_ptr(), tout.data_ptr(), n, 0, sp) == 0
-            torch.cuda.synchronize()
-            print(json.dumps({"mode": "profile", "n": n, "sorts": args.warmup + 1}), flush=True)
-            return 0
+            return profile_run(lib, orc, args)
         if args.mode == "trace":
             res = host_trace(lib, gms, orc, args.n, args.warmup, args.trace_out)
         elif args.mode == "batched":

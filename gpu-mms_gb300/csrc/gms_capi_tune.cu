@@ -91,8 +91,8 @@ std::string table_json_locked() {
     const TuneEntry& e = g_table[i];
     snprintf(buf, sizeof(buf),
              "%s{\"dtype\": %d, \"kv\": %d, \"log2n\": %d, \"k\": %d, \"sample_b\": %d, \"bulk_copy\": %d, "
-             "\"ms\": %.4f}",
-             i ? ", " : "", e.dtype, e.kv, e.cls, e.t.k, e.t.sample_b, e.t.bulk_copy, e.ms);
+             "\"split\": %d, \"ms\": %.4f}",
+             i ? ", " : "", e.dtype, e.kv, e.cls, e.t.k, e.t.sample_b, e.t.bulk_copy, e.t.split, e.ms);
     out += buf;
   }
   return out + "]";
@@ -139,13 +139,16 @@ int load_cache(const char* path) {
         !field_num(p, q, "k", &k) || !field_num(p, q, "sample_b", &sb) || !field_num(p, q, "bulk_copy", &bulk))
       return set_error(GMS_ERR_INVALID, "tune cache: entry lacks a field");
     field_num(p, q, "ms", &ms);
+    double split = 0;  // optional (files written before the splitter choice existed lack it)
+    field_num(p, q, "split", &split);
     if (dt < 0 || dt > 5 || (kv != 0 && kv != 1) || cls < 0 || cls > 40 || !valid_tune((int)k, (int)sb) ||
-        bulk < 0 || bulk > 3)
+        bulk < 0 || bulk > 3 || (split != 0 && split != 1))
       return set_error(GMS_ERR_INVALID, "tune cache: entry out of range");
     gms::Tune t;
     t.k = (int)k;
     t.sample_b = (int)sb;
     t.bulk_copy = (int)bulk;
+    t.split = (int)split;
     got.push_back(TuneEntry{(int)dt, (int)kv, (int)cls, t, ms});
     pos = b + 1;
   }
@@ -274,7 +277,27 @@ int gms_set_tune(int k, int sample_b, int bulk_copy) {
   g_tune.k = k;
   g_tune.sample_b = sample_b;
   g_tune.bulk_copy = bulk_copy;
+  g_tune.split = 0;
   g_tune_explicit = true;
+  return GMS_OK;
+}
+
+int gms_set_tune_ex(int k, int sample_b, int bulk_copy, int split) {
+  clear_error();
+  if (split != 0 && split != 1) return set_error(GMS_ERR_INVALID, "split must be 0 or 1");
+  const int rc = gms_set_tune(k, sample_b, bulk_copy);
+  if (rc != GMS_OK) return rc;
+  std::lock_guard<std::mutex> g(g_tune_mu);
+  g_tune.split = split;
+  return GMS_OK;
+}
+
+int gms_get_tune_ex(int* k, int* sample_b, int* bulk_copy, int* split) {
+  std::lock_guard<std::mutex> g(g_tune_mu);
+  if (k) *k = g_tune.k;
+  if (sample_b) *sample_b = g_tune.sample_b;
+  if (bulk_copy) *bulk_copy = g_tune.bulk_copy;
+  if (split) *split = g_tune.split;
   return GMS_OK;
 }
 
@@ -353,7 +376,9 @@ int gms_autotune(int dtype, int kv, int64_t n, void* stream, int* out_k, int* ou
   double best_ms = 1e30;
   gms::Tune best;
   bool have_first = false;
-  for (const gms::Tune& t : cands) {
+  // stage 1: every candidate above; stage 2: the best one with the direct
+  // (findPartitions-style) splitter instead of the sample-bracketed one
+  auto try_tune = [&](const gms::Tune& t) -> int {
     OverrideScope scope(&t);
     auto one = [&]() -> int {
       cudaMemcpyAsync(b.p[2], b.p[0], kb, cudaMemcpyDeviceToDevice, st);
@@ -363,7 +388,7 @@ int gms_autotune(int dtype, int kv, int64_t n, void* stream, int* out_k, int* ou
       cudaEventRecord(b.ev[1], st);
       return rc;
     };
-    if (one() != GMS_OK) continue;  // a tuning too fine for this n: not a candidate
+    if (one() != GMS_OK) return GMS_OK;  // a tuning too fine for this n: not a candidate
     // Every tuning must give the same bits (the result of a sort is unique).
     if (!have_first) {
       cudaMemcpyAsync(b.p[6], b.p[4], kb, cudaMemcpyDeviceToDevice, st);
@@ -396,6 +421,17 @@ int gms_autotune(int dtype, int kv, int64_t n, void* stream, int* out_k, int* ou
       best_ms = med;
       best = t;
     }
+    return GMS_OK;
+  };
+  for (const gms::Tune& t : cands) {
+    const int rc = try_tune(t);
+    if (rc != GMS_OK) return rc;
+  }
+  if (have_first && gms_rounds(dtype, kv, n) > 0) {
+    gms::Tune t2 = best;
+    t2.split = 1;
+    const int rc = try_tune(t2);
+    if (rc != GMS_OK) return rc;
   }
   if (!have_first) return set_error(GMS_ERR_INTERNAL, "no tuning candidate ran");
   int flag = 0;

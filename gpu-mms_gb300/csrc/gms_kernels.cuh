@@ -1148,6 +1148,10 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
 // Segmented rounds (grp set): row r belongs to group row_grp[r]; the group's
 // runs, block samples and merged sample follow its GroupDesc, and GRP_ALT
 // groups read `data2`.
+// direct = 1 (a tuning alternative): each lane binary-searches its whole run
+// for the boundary key, as the reference's findPartitions does
+// (warp-partition.hxx:488-532), instead of first bracketing the answer to one
+// block with the run's block sample.
 template <class KeyT, class Cmp, class Codec>
 __global__ void __launch_bounds__(256) splitter_kernel(const KeyT* __restrict__ data, const KeyT* __restrict__ samp,
                                                         const KeyT* __restrict__ fkeys,
@@ -1157,7 +1161,7 @@ __global__ void __launch_bounds__(256) splitter_kernel(const KeyT* __restrict__ 
                                                         int64_t* __restrict__ desc, int64_t* __restrict__ doff,
                                                         int enc, const GroupDesc* __restrict__ grp,
                                                         const int32_t* __restrict__ row_grp,
-                                                        const KeyT* __restrict__ data2) {
+                                                        const KeyT* __restrict__ data2, int direct) {
   const Cmp cmp;
   const int lane = threadIdx.x & 31;
   const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -1206,26 +1210,36 @@ __global__ void __launch_bounds__(256) splitter_kernel(const KeyT* __restrict__ 
         // (lane < kb) or key < v (lane > kb)
         const bool le = lane < kb;
         auto precedes = [=](const KeyT& x) -> bool { return le ? !cmp(v, x) : cmp(x, v); };
-        // 1. blocks whose first key precedes the boundary
-        const KeyT* sr = samp + (run0 + lane) * sample_run_len;
-        const int64_t nb = (len + sample_b - 1) / sample_b;
-        int64_t lo = 0, hi = nb;
-        while (lo < hi) {
-          const int64_t mid = (lo + hi) >> 1;
-          if (precedes(sr[mid])) lo = mid + 1; else hi = mid;
-        }
-        // 2. inside the last such block
-        if (lo == 0) {
-          c = 0;
-        } else {
+        if (direct) {
           const KeyT* r = data + gbase + rs;
-          int64_t a0 = (lo - 1) * sample_b + 1;
-          int64_t a1 = min64(lo * (int64_t)sample_b, len);
+          int64_t a0 = 0, a1 = len;
           while (a0 < a1) {
             const int64_t mid = (a0 + a1) >> 1;
             if (precedes(maybe_enc<Codec>(r[mid], enc))) a0 = mid + 1; else a1 = mid;
           }
           c = a0;
+        } else {
+          // 1. blocks whose first key precedes the boundary
+          const KeyT* sr = samp + (run0 + lane) * sample_run_len;
+          const int64_t nb = (len + sample_b - 1) / sample_b;
+          int64_t lo = 0, hi = nb;
+          while (lo < hi) {
+            const int64_t mid = (lo + hi) >> 1;
+            if (precedes(sr[mid])) lo = mid + 1; else hi = mid;
+          }
+          // 2. inside the last such block
+          if (lo == 0) {
+            c = 0;
+          } else {
+            const KeyT* r = data + gbase + rs;
+            int64_t a0 = (lo - 1) * sample_b + 1;
+            int64_t a1 = min64(lo * (int64_t)sample_b, len);
+            while (a0 < a1) {
+              const int64_t mid = (a0 + a1) >> 1;
+              if (precedes(maybe_enc<Codec>(r[mid], enc))) a0 = mid + 1; else a1 = mid;
+            }
+            c = a0;
+          }
         }
       }
     }

@@ -71,6 +71,8 @@ struct Tune {
   int sample_b = 32;  // block size of the forecast sample
   int bulk_copy = 1;  // tile staging: 1 cp.async.bulk by one warp (3: same, persistent CTAs overlapping the
                       // next tile's staging with the store); 2 cp.async by every warp; 0 plain loads
+  int split = 0;      // tile boundaries: 0 the block sample brackets each run's co-rank to one block, then a
+                      // search inside it; 1 a binary search over the whole run (findPartitions-style)
 };
 
 // Scratch layout, computed by a dry run of the same recursion as the real run.
@@ -581,7 +583,7 @@ struct Engine {
       hook_before(KC_SPLIT, st);
       splitter_kernel<KeyT, Cmp, Codec><<<(unsigned)ceil_div(threads, 256), 256, 0, st>>>(
           in, S, w.fk[level + 1], w.fi[level + 1], n, L, k, Ls, sb, G, tiles_full, tiles_last, groups, w.desc[level],
-          w.doff[level], enc, sl ? sl->grp : nullptr, sl ? sl->row_grp : nullptr, in2);
+          w.doff[level], enc, sl ? sl->grp : nullptr, sl ? sl->row_grp : nullptr, in2, t.split);
       e = cudaGetLastError();
       hook_after(KC_SPLIT, st);
       if (e != cudaSuccess) return e;

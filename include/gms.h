@@ -374,6 +374,14 @@ int gms_timing_reset(void);
 int gms_set_tune(int k, int sample_b, int bulk_copy);
 int gms_get_tune(int* k, int* sample_b, int* bulk_copy);
 int gms_clear_tune(void);
+/* The same with the splitter, the reference's PIVOT_MOVES switch between
+ * partition strategies (src/params.h:21, src/warp-partition.hxx:179-470):
+ *   split 0  each run's co-rank at a tile boundary bracketed to one block by
+ *            the run's block sample, then searched inside it (default);
+ *   split 1  a binary search over the whole run, as findPartitions does.
+ * gms_set_tune sets split 0.  The autotuner tries split 1 on its best tuning. */
+int gms_set_tune_ex(int k, int sample_b, int bulk_copy, int split);
+int gms_get_tune_ex(int* k, int* sample_b, int* bulk_copy, int* split);
 
 /* ---------------------------------------------------------------------------
  * Autotuner.  No reference counterpart beyond the sweep scripts named above:

@@ -91,3 +91,35 @@ def test_workspace_size_grows_with_n(lib):
     assert sizes[-1] < (1 << 28) * 4 // 4
     assert lib.gms_workspace_bytes(0, 0, 0) == 0
     assert lib.gms_workspace_bytes(4, 1, 1 << 20) > lib.gms_workspace_bytes(0, 0, 1 << 20)
+
+
+def test_splitter_choice(lib):
+    """gms_set_tune_ex carries the splitter (the reference's partition
+    strategy switch); gms_set_tune resets it to the block-sample splitter."""
+    q = [ctypes.c_int() for _ in range(4)]
+
+    def get_ex():
+        assert lib.gms_get_tune_ex(*[ctypes.byref(x) for x in q]) == GMS_OK
+        return tuple(x.value for x in q)
+
+    try:
+        assert lib.gms_set_tune_ex(32, 32, 1, 1) == GMS_OK
+        assert get_ex() == (32, 32, 1, 1)
+        assert lib.gms_set_tune_ex(32, 32, 1, 2) == GMS_ERR_INVALID
+        assert b"split" in lib.gms_last_error()
+        assert get_ex() == (32, 32, 1, 1)
+        assert lib.gms_set_tune(16, 32, 3) == GMS_OK
+        assert get_ex() == (16, 32, 3, 0)
+    finally:
+        lib.gms_clear_tune()
+
+
+def test_segmented_argument_checks(lib):
+    vp = ctypes.c_void_p
+    # nothing to sort, or bad sizes, before any device work
+    assert lib.gms_segmented_sort_i32(None, None, 0, None, 0, None) == GMS_OK
+    assert lib.gms_segmented_sort_i32(None, None, -1, None, 1, None) == GMS_ERR_INVALID
+    assert lib.gms_segmented_sort_u64(vp(16), vp(16), 10, None, 1, None) == GMS_ERR_INVALID
+    assert b"null" in lib.gms_last_error()
+    assert lib.gms_segmented_sort_kv_u64_i32(vp(16), None, vp(16), vp(16), 10, vp(16), 1, None) == GMS_ERR_INVALID
+    assert lib.gms_segmented_sort_i32(vp(16), vp(16), 10, vp(16), 0, None) == GMS_ERR_INVALID
