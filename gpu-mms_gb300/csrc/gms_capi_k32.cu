@@ -155,11 +155,12 @@ int host_sort_enqueue(const int32_t* host_in, int32_t* host_out, int64_t n, cuda
   }
   // Up to kChunks pieces of whole base tiles (host_chunk_plan), the first one small
   // so that the sort starts soon after the call.
-  const int64_t tiles = gms::ceil_div(n, EngI32::BASE_TILE);
   const gms::Tune tune = tune_for(0, 0, n);
+  const int64_t bt = EngI32::base_tile(tune);
+  const int64_t tiles = gms::ceil_div(n, bt);
   int64_t* start = p->start[slot];
   gms::BaseGate gate;
-  gate.chunks = gms::host_chunk_plan(tiles, tune.k, EngI32::passes_for(n, tune.k), start);
+  gate.chunks = gms::host_chunk_plan(tiles, tune.k, EngI32::passes_for(n, tune), start);
   gate.start = start;
   gate.ready = p->ready[slot];
   gate.early_rounds = sync;
@@ -171,8 +172,8 @@ int host_sort_enqueue(const int32_t* host_in, int32_t* host_out, int64_t n, cuda
     gate.join = p->join;
   }
   for (int c = 0; c < gate.chunks; ++c) {
-    const int64_t k0 = std::min(n, start[c] * EngI32::BASE_TILE);
-    const int64_t k1 = std::min(n, start[c + 1] * EngI32::BASE_TILE);
+    const int64_t k0 = std::min(n, start[c] * bt);
+    const int64_t k1 = std::min(n, start[c + 1] * bt);
     if (k1 > k0) {
       gms::hook_before(gms::KC_H2D, p->h2d);
       e = cudaMemcpyAsync((int32_t*)p->din[slot] + k0, host_in + k0, sizeof(int32_t) * (size_t)(k1 - k0),

@@ -254,10 +254,10 @@ int64_t gms_base_tile(int dtype, int kv) {
 }
 
 int gms_rounds(int dtype, int kv, int64_t n) {
-  int p = 0;
-  const int k = tune_for(dtype, kv, n).k;
-  for (int64_t L = gms_base_tile(dtype, kv); L < n; L *= k) ++p;
-  return p;
+  const gms::Tune t = tune_for(dtype, kv, n);
+  if (kv) return KvEngine<uint32_t, gms::IdentityCodec<uint32_t>>::passes_for(n, t);
+  if (dtype >= 3) return KeysEngine<uint64_t, gms::IdentityCodec<uint64_t>>::passes_for(n, t);
+  return KeysEngine<uint32_t, gms::IdentityCodec<uint32_t>>::passes_for(n, t);
 }
 
 size_t gms_workspace_bytes(int dtype, int kv, int64_t n) {

@@ -91,8 +91,8 @@ std::string table_json_locked() {
     const TuneEntry& e = g_table[i];
     snprintf(buf, sizeof(buf),
              "%s{\"dtype\": %d, \"kv\": %d, \"log2n\": %d, \"k\": %d, \"sample_b\": %d, \"bulk_copy\": %d, "
-             "\"split\": %d, \"ms\": %.4f}",
-             i ? ", " : "", e.dtype, e.kv, e.cls, e.t.k, e.t.sample_b, e.t.bulk_copy, e.t.split, e.ms);
+             "\"split\": %d, \"base\": %d, \"ms\": %.4f}",
+             i ? ", " : "", e.dtype, e.kv, e.cls, e.t.k, e.t.sample_b, e.t.bulk_copy, e.t.split, e.t.base, e.ms);
     out += buf;
   }
   return out + "]";
@@ -139,16 +139,18 @@ int load_cache(const char* path) {
         !field_num(p, q, "k", &k) || !field_num(p, q, "sample_b", &sb) || !field_num(p, q, "bulk_copy", &bulk))
       return set_error(GMS_ERR_INVALID, "tune cache: entry lacks a field");
     field_num(p, q, "ms", &ms);
-    double split = 0;  // optional (files written before the splitter choice existed lack it)
+    double split = 0, base = 0;  // optional (files written before these choices existed lack them)
     field_num(p, q, "split", &split);
+    field_num(p, q, "base", &base);
     if (dt < 0 || dt > 5 || (kv != 0 && kv != 1) || cls < 0 || cls > 40 || !valid_tune((int)k, (int)sb) ||
-        bulk < 0 || bulk > 3 || (split != 0 && split != 1))
+        bulk < 0 || bulk > 3 || (split != 0 && split != 1) || (base != 0 && base != 1))
       return set_error(GMS_ERR_INVALID, "tune cache: entry out of range");
     gms::Tune t;
     t.k = (int)k;
     t.sample_b = (int)sb;
     t.bulk_copy = (int)bulk;
     t.split = (int)split;
+    t.base = (int)base;
     got.push_back(TuneEntry{(int)dt, (int)kv, (int)cls, t, ms});
     pos = b + 1;
   }
@@ -278,26 +280,30 @@ int gms_set_tune(int k, int sample_b, int bulk_copy) {
   g_tune.sample_b = sample_b;
   g_tune.bulk_copy = bulk_copy;
   g_tune.split = 0;
+  g_tune.base = 0;
   g_tune_explicit = true;
   return GMS_OK;
 }
 
-int gms_set_tune_ex(int k, int sample_b, int bulk_copy, int split) {
+int gms_set_tune_ex(int k, int sample_b, int bulk_copy, int split, int base) {
   clear_error();
   if (split != 0 && split != 1) return set_error(GMS_ERR_INVALID, "split must be 0 or 1");
+  if (base != 0 && base != 1) return set_error(GMS_ERR_INVALID, "base must be 0 or 1");
   const int rc = gms_set_tune(k, sample_b, bulk_copy);
   if (rc != GMS_OK) return rc;
   std::lock_guard<std::mutex> g(g_tune_mu);
   g_tune.split = split;
+  g_tune.base = base;
   return GMS_OK;
 }
 
-int gms_get_tune_ex(int* k, int* sample_b, int* bulk_copy, int* split) {
+int gms_get_tune_ex(int* k, int* sample_b, int* bulk_copy, int* split, int* base) {
   std::lock_guard<std::mutex> g(g_tune_mu);
   if (k) *k = g_tune.k;
   if (sample_b) *sample_b = g_tune.sample_b;
   if (bulk_copy) *bulk_copy = g_tune.bulk_copy;
   if (split) *split = g_tune.split;
+  if (base) *base = g_tune.base;
   return GMS_OK;
 }
 
@@ -377,7 +383,8 @@ int gms_autotune(int dtype, int kv, int64_t n, void* stream, int* out_k, int* ou
   gms::Tune best;
   bool have_first = false;
   // stage 1: every candidate above; stage 2: the best one with the direct
-  // (findPartitions-style) splitter instead of the sample-bracketed one
+  // (findPartitions-style) splitter instead of the sample-bracketed one;
+  // stage 3: the other base case
   auto try_tune = [&](const gms::Tune& t) -> int {
     OverrideScope scope(&t);
     auto one = [&]() -> int {
@@ -431,6 +438,14 @@ int gms_autotune(int dtype, int kv, int64_t n, void* stream, int* out_k, int* ou
     gms::Tune t2 = best;
     t2.split = 1;
     const int rc = try_tune(t2);
+    if (rc != GMS_OK) return rc;
+  }
+  // stage 3 (keys-only sorts): the per-thread base case instead of the
+  // warp-shuffle one, with the best tuning so far
+  if (have_first && !kv) {
+    gms::Tune t3 = best;
+    t3.base = 1;
+    const int rc = try_tune(t3);
     if (rc != GMS_OK) return rc;
   }
   if (!have_first) return set_error(GMS_ERR_INTERNAL, "no tuning candidate ran");

@@ -285,6 +285,10 @@ __global__ void __launch_bounds__(NT, (MODE == MODE_BASE && sizeof(KeyT) == 4 &&
     }
     __syncthreads();
     // Merge levels up to the whole (padded) tile, ping-ponging the buffers.
+    // Runs of rl = ITEMS * 2^lv keys: pair p (2 * rl keys) gets exactly
+    // 2 * rl / ITEMS threads, so every window is full and none crosses a
+    // pair's end (window-aligned merges, no pair lookup per output).
+    static_assert((NT & (NT - 1)) == 0, "the base tile's merge levels need a power-of-two thread count");
     for (int rl = ITEMS; rl < CAP; rl *= 2) {
       const KeyT* xk = (cur ? k1 : k0);
       KeyT* yk = (cur ? k0 : k1);
@@ -293,11 +297,16 @@ __global__ void __launch_bounds__(NT, (MODE == MODE_BASE && sizeof(KeyT) == 4 &&
       const PlainLoad<KeyT> ld(xk);
       const SmemArray<KeyT> yka(yk + s);
       const SmemArray<V> xva(xv), yva(yv + s);
-      const RegularPairs pairs{rl, CAP};
-      merge_thread<ITEMS, KeyT>(s, ld, cmp, pairs, [&](int i, KeyT k, uint32_t src, bool, const PairRange&) {
-        yka.put(i, k);
-        if constexpr (kHasVal) yva.put(i, xva.get((int)((src - ld.base) / (uint32_t)sizeof(KeyT))));
-      });
+      const int tpp = 2 * rl / ITEMS;
+      const int p = tid / tpp;
+      const int diag = (tid - p * tpp) * ITEMS;
+      const int ps = p * 2 * rl;
+      merge_window<ITEMS, KeyT, 2, 1>(ld, cmp, ld.addr(ps), rl, ld.addr(ps + rl), rl, diag, ITEMS, 0xffffffffu,
+                                      [&](int i, KeyT k, uint32_t src, bool) {
+                                        yka.put(i, k);
+                                        if constexpr (kHasVal)
+                                          yva.put(i, xva.get((int)((src - ld.base) / (uint32_t)sizeof(KeyT))));
+                                      });
       __syncthreads();
       cur ^= 1;
     }

@@ -73,6 +73,9 @@ struct Tune {
                       // next tile's staging with the store); 2 cp.async by every warp; 0 plain loads
   int split = 0;      // tile boundaries: 0 the block sample brackets each run's co-rank to one block, then a
                       // search inside it; 1 a binary search over the whole run (findPartitions-style)
+  int base = 0;       // base case of keys-only integer sorts: 0 register network + warp-shuffle merges (8192-key
+                      // tiles for 32-bit keys); 1 register network per thread + shared-memory merge levels
+                      // (the engine's NT x ITEMS tile); other engines always use the latter
 };
 
 // Scratch layout, computed by a dry run of the same recursion as the real run.
@@ -380,9 +383,12 @@ struct Engine {
   static constexpr int BASE_TILE = kWarpBase ? kNTB * kKPL : CAP;
 
   // ---------------- geometry ----------------
-  static int passes_for(int64_t n, int k) {
+  // the base case a tuning selects, and its tile
+  static bool warp_base(const Tune& t) { return kWarpBase && t.base == 0; }
+  static int64_t base_tile(const Tune& t) { return warp_base(t) ? (int64_t)BASE_TILE : (int64_t)CAP; }
+  static int passes_for(int64_t n, const Tune& t) {
     int p = 0;
-    for (int64_t L = BASE_TILE; L < n; L *= k) ++p;
+    for (int64_t L = base_tile(t); L < n; L *= t.k) ++p;
     return p;
   }
 
@@ -417,7 +423,7 @@ struct Engine {
 
   static WsLayout plan(int64_t n, const Tune& t) {
     WsLayout l;
-    int64_t L = BASE_TILE;
+    int64_t L = base_tile(t);
     while (L < n) {
       plan_round<V>(l, 0, n, L, t);
       L *= t.k;
@@ -620,7 +626,7 @@ struct Engine {
   // the last round lands in `out`.
   static cudaError_t sort(const WsPtrs<KeyT>& w, KeyT* in, V* vin, KeyT* out, V* vout, int64_t n, const Tune& t,
                           cudaStream_t st, const BaseGate* gate = nullptr, const RoundSplit* split = nullptr) {
-    const bool odd = passes_for(n, t.k) % 2 == 1;
+    const bool odd = passes_for(n, t) % 2 == 1;
     return sort_to(w, in, vin, odd ? in : out, odd ? vin : vout, odd ? out : in, odd ? vout : vin, out, vout, n, t, st,
                    gate, split);
   }
@@ -635,7 +641,8 @@ struct Engine {
                              KeyT* dst, V* vdst, int64_t n, const Tune& t, cudaStream_t st,
                              const BaseGate* gate = nullptr, const RoundSplit* split = nullptr) {
     if (n <= 0) return cudaSuccess;
-    const int P = passes_for(n, t.k);
+    const int P = passes_for(n, t);
+    const int64_t bt = base_tile(t);
     KeyT* buf[2] = {d0, d1};
     V* vbuf[2] = {vd0, vd1};
     int rounds_done = 0;  // rounds already run chunk by chunk
@@ -646,18 +653,18 @@ struct Engine {
       a.vin = vsrc;
       a.vout = P > 0 ? vd0 : vdst;
       a.n = n;
-      a.L = BASE_TILE;
+      a.L = bt;
       a.k = 1;
       a.enc_on_load = 1;
       a.dec_on_store = (P == 0) ? 1 : 0;
       a.gen_index = 0;
       a.err = w.err;
       a.sample_b = t.sample_b;
-      a.out_run_len = BASE_TILE;
-      a.sample_run_len = ceil_div(BASE_TILE, t.sample_b);
+      a.out_run_len = bt;
+      a.sample_run_len = ceil_div(bt, t.sample_b);
       a.sample_out = (P > 0) ? w.s1[0] : nullptr;
       cudaError_t e = cudaSuccess;
-      if constexpr (kWarpBase) {
+      if (warp_base(t)) {
         const int64_t tiles = ceil_div(n, BASE_TILE);
         if (!gate) {
           e = launch_base_warp(a, tiles, st);
@@ -730,7 +737,7 @@ struct Engine {
     }
     int cur = rounds_done & 1;
     int sbuf = rounds_done & 1;
-    int64_t L = BASE_TILE;
+    int64_t L = bt;
     for (int p = 0; p < rounds_done; ++p) L *= t.k;
     for (int p = rounds_done; p < P; ++p) {
       const bool last = (p == P - 1);
@@ -750,7 +757,7 @@ struct Engine {
   // ---------------- segmented sorts ----------------
   static SegGeom seg_geom(const Tune& t) {
     SegGeom g;
-    g.base_tile = BASE_TILE;
+    g.base_tile = base_tile(t);
     g.cap_data = Geo<V>::CAP;
     g.capw_data = Geo<V>::CAPW;
     g.cap_idx = Geo<IdxT>::CAP;
@@ -781,25 +788,21 @@ struct Engine {
     a.out2 = dst;
     a.vin2 = vsrc;
     a.vout2 = vdst;
+    const int64_t bt = base_tile(t);
     a.n = n;
-    a.L = BASE_TILE;
+    a.L = bt;
     a.k = 1;
     a.enc_on_load = 1;
     a.dec_on_store = 0;
     a.err = w.err;
     a.grp = D.base;
     a.sample_b = t.sample_b;
-    a.out_run_len = BASE_TILE;
-    a.sample_run_len = ceil_div(BASE_TILE, t.sample_b);
+    a.out_run_len = bt;
+    a.sample_run_len = ceil_div(bt, t.sample_b);
     a.sample_out = R > 0 ? w.s1[0] : nullptr;
-    cudaError_t e;
-    if constexpr (kWarpBase) {
-      e = launch_base_warp(a, D.base_tiles, st);
-    } else {
-      e = launch_tile<MODE_BASE>(a, D.base_tiles, st);
-    }
+    cudaError_t e = warp_base(t) ? launch_base_warp(a, D.base_tiles, st) : launch_tile<MODE_BASE>(a, D.base_tiles, st);
     if (e != cudaSuccess) return e;
-    int64_t L = BASE_TILE;
+    int64_t L = bt;
     for (int p = 0; p < R; ++p, L *= t.k) {
       const SegLevelDev* sl = &D.levels[(size_t)D.rounds[(size_t)p]];
       KeyT* sout = (p + 1 < R) ? w.s1[(p + 1) & 1] : nullptr;

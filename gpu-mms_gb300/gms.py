@@ -196,8 +196,8 @@ SIGNATURES = {
     "gms_launch_count": (ctypes.c_longlong, []),
     "gms_set_tune": (_i32, [_i32, _i32, _i32]),
     "gms_get_tune": (_i32, [ctypes.POINTER(ctypes.c_int)] * 3),
-    "gms_set_tune_ex": (_i32, [_i32, _i32, _i32, _i32]),
-    "gms_get_tune_ex": (_i32, [ctypes.POINTER(ctypes.c_int)] * 4),
+    "gms_set_tune_ex": (_i32, [_i32, _i32, _i32, _i32, _i32]),
+    "gms_get_tune_ex": (_i32, [ctypes.POINTER(ctypes.c_int)] * 5),
     "gms_clear_tune": (_i32, []),
     "gms_autotune": (_i32, [_i32, _i32, _i64, _vp] + [ctypes.POINTER(ctypes.c_int)] * 3
                      + [ctypes.POINTER(ctypes.c_double)]),

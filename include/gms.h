@@ -374,14 +374,23 @@ int gms_timing_reset(void);
 int gms_set_tune(int k, int sample_b, int bulk_copy);
 int gms_get_tune(int* k, int* sample_b, int* bulk_copy);
 int gms_clear_tune(void);
-/* The same with the splitter, the reference's PIVOT_MOVES switch between
- * partition strategies (src/params.h:21, src/warp-partition.hxx:179-470):
- *   split 0  each run's co-rank at a tile boundary bracketed to one block by
- *            the run's block sample, then searched inside it (default);
- *   split 1  a binary search over the whole run, as findPartitions does.
- * gms_set_tune sets split 0.  The autotuner tries split 1 on its best tuning. */
-int gms_set_tune_ex(int k, int sample_b, int bulk_copy, int split);
-int gms_get_tune_ex(int* k, int* sample_b, int* bulk_copy, int* split);
+/* The same with two strategy switches, the counterparts of the reference's
+ * compile-time alternatives:
+ *   split  tile boundaries (PIVOT_MOVES, src/params.h:21; the partition
+ *          strategies of src/warp-partition.hxx:179-470):
+ *            0  each run's co-rank bracketed to one block by the run's block
+ *               sample, then searched inside it (default);
+ *            1  a binary search over the whole run, as findPartitions does;
+ *   base   base case of keys-only sorts (the base-case variants of
+ *          src/basecase/squareSort.hxx:62-131, sortRowMajor.hxx:341-392):
+ *            0  register network per lane + warp-shuffle merges + shared-memory
+ *               levels, 8192-key tiles for 32-bit keys (default);
+ *            1  register network per thread + shared-memory merge levels,
+ *               8704-key tiles (the base case of the payload engines).
+ * gms_set_tune sets both to 0.  The autotuner tries split 1 and then base 1
+ * on its best tuning. */
+int gms_set_tune_ex(int k, int sample_b, int bulk_copy, int split, int base);
+int gms_get_tune_ex(int* k, int* sample_b, int* bulk_copy, int* split, int* base);
 
 /* ---------------------------------------------------------------------------
  * Autotuner.  No reference counterpart beyond the sweep scripts named above:

@@ -93,23 +93,29 @@ def test_workspace_size_grows_with_n(lib):
     assert lib.gms_workspace_bytes(4, 1, 1 << 20) > lib.gms_workspace_bytes(0, 0, 1 << 20)
 
 
-def test_splitter_choice(lib):
-    """gms_set_tune_ex carries the splitter (the reference's partition
-    strategy switch); gms_set_tune resets it to the block-sample splitter."""
-    q = [ctypes.c_int() for _ in range(4)]
+def test_strategy_choices(lib):
+    """gms_set_tune_ex carries the splitter and base-case strategies (the
+    reference's compile-time alternatives); gms_set_tune resets both."""
+    q = [ctypes.c_int() for _ in range(5)]
 
     def get_ex():
         assert lib.gms_get_tune_ex(*[ctypes.byref(x) for x in q]) == GMS_OK
         return tuple(x.value for x in q)
 
     try:
-        assert lib.gms_set_tune_ex(32, 32, 1, 1) == GMS_OK
-        assert get_ex() == (32, 32, 1, 1)
-        assert lib.gms_set_tune_ex(32, 32, 1, 2) == GMS_ERR_INVALID
+        assert lib.gms_set_tune_ex(32, 32, 1, 1, 1) == GMS_OK
+        assert get_ex() == (32, 32, 1, 1, 1)
+        # the per-thread base case has 8704-key tiles: 2^28 keys still take 3 rounds
+        assert lib.gms_rounds(0, 0, 1 << 28) == 3
+        assert lib.gms_rounds(0, 0, 8704) == 0 and lib.gms_rounds(0, 0, 8705) == 1
+        assert lib.gms_set_tune_ex(32, 32, 1, 2, 0) == GMS_ERR_INVALID
         assert b"split" in lib.gms_last_error()
-        assert get_ex() == (32, 32, 1, 1)
+        assert lib.gms_set_tune_ex(32, 32, 1, 0, 2) == GMS_ERR_INVALID
+        assert b"base" in lib.gms_last_error()
+        assert get_ex() == (32, 32, 1, 1, 1)
         assert lib.gms_set_tune(16, 32, 3) == GMS_OK
-        assert get_ex() == (16, 32, 3, 0)
+        assert get_ex() == (16, 32, 3, 0, 0)
+        assert lib.gms_rounds(0, 0, 8193) == 1
     finally:
         lib.gms_clear_tune()
 

@@ -272,6 +272,39 @@ def test_tune_variants(gms, oracle, tuned, k, b, bulk):
     assert_same(gv, ov_, "kv payload")
 
 
+# The strategy switches (the reference's compile-time alternatives): the
+# direct findPartitions-style splitter and the per-thread base case, alone and
+# together, on 32- and 64-bit keys, keys only and with a payload, and batched.
+@pytest.mark.parametrize("split,base", [(1, 0), (0, 1), (1, 1)])
+def test_strategy_variants(gms, oracle, tuned, split, base):
+    lib = tuned
+    assert lib.gms_set_tune_ex(32, 32, 1, split, base) == 0, lib.gms_last_error()
+    for n, dist in [(8704, 0), (8705, 6), (300001, 0), (2_500_001, 4), (3_000_003, 5)]:
+        a = oracle.gen_i32(n, dist, 3 + split + 2 * base)
+        assert_same(gpu_sort(gms, a), oracle.sort(a), f"split={split} base={base} n={n} dist={dist}")
+    u = oracle.gen_u64(1_000_003, 9)
+    assert_same(gpu_sort(gms, u), oracle.sort(u), "u64")
+    k64 = oracle.gen_u64(700001, 4)
+    v = np.arange(k64.size, dtype=np.int32)
+    k64[::3] = k64[1]
+    gk, gv = gpu_sort_kv(gms, k64, v)
+    ok_, ov_ = oracle.sort_kv(k64, v)
+    assert_same(gk, ok_, "kv keys")
+    assert_same(gv, ov_, "kv payload")
+    # a batch of arrays under the same strategies
+    lengths = np.array([1, 8704, 8705, 300000, 0, 4000, 1_200_000], dtype=np.int64)
+    off = np.zeros(len(lengths) + 1, dtype=np.int64)
+    np.cumsum(lengths, out=off[1:])
+    keys = oracle.gen_i32(int(off[-1]), 0, 5)
+    tin = torch.from_numpy(keys).cuda()
+    tout = torch.empty_like(tin)
+    toff = torch.from_numpy(off).cuda()
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assert lib.gms_segmented_sort_i32(tin.data_ptr(), tout.data_ptr(), keys.size, toff.data_ptr(), len(lengths),
+                                      st) == 0, lib.gms_last_error()
+    assert_same(tout.cpu().numpy(), oracle.segmented_sort(keys, off), "batched")
+
+
 def test_tune_rejects_bad_values(gms, tuned):
     lib = tuned
     assert lib.gms_set_tune(1, 32, 1) == 1
