@@ -261,6 +261,11 @@ __device__ __forceinline__ void sts(uint32_t addr, const T& x) {
   }
 }
 
+// 16-byte shared store of four 32-bit words (the address 16-byte aligned).
+__device__ __forceinline__ void sts_v4(uint32_t addr, uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
+  asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(a), "r"(b), "r"(c), "r"(d) : "memory");
+}
+
 // Loaders.  Keys are addressed by 32-bit shared-window BYTE addresses, so a
 // merge step advances a pointer by sizeof(KeyT) and loads at an immediate
 // offset, with no index multiply.  PlainLoad reads keys as stored; EncLoad

@@ -539,9 +539,42 @@ __global__ void __launch_bounds__(NT) base_warp_kernel(TileArgs<KeyT, NoVal> a0)
   // sentinels.
   {
     KeyT* run = k0 + warp * (Geo::WARP_RUN + PAD);
-    const SmemArray<KeyT> dst(run + lane * KPL);
+    constexpr int KPC = 16 / (int)sizeof(KeyT);  // keys per 16-byte chunk
+    constexpr int NC = KPL / KPC;                // chunks per lane
+    if constexpr (NC == 8 && ((Geo::WARP_RUN + PAD) * sizeof(KeyT)) % 16 == 0) {
+      // A lane's run is 128 bytes, so the same store of every lane would hit
+      // the same banks.  Lane l writes its chunk c ^ (l & 7) at step c
+      // instead: the eight lanes of a quarter-warp then write eight
+      // different bank groups (conflict-free 16-byte stores).  The chunks
+      // are XOR-permuted in registers first (three conditional swaps).
+      const int t = lane & 7;
 #pragma unroll
-    for (int r = 0; r < KPL; ++r) dst.put(r, x[r]);
+      for (int b = 1; b < NC; b <<= 1) {
+        const bool sw = (t & b) != 0;
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+          if ((c & b) == 0) {
+#pragma unroll
+            for (int e = 0; e < KPC; ++e) {
+              const KeyT u = x[c * KPC + e], v = x[(c ^ b) * KPC + e];
+              x[c * KPC + e] = sw ? v : u;
+              x[(c ^ b) * KPC + e] = sw ? u : v;
+            }
+          }
+        }
+      }
+      const uint32_t base = static_cast<uint32_t>(__cvta_generic_to_shared(run)) + 128u * (uint32_t)lane;
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        uint32_t w[4];
+        memcpy(w, &x[c * KPC], 16);
+        sts_v4(base + 16u * (uint32_t)(c ^ t), w[0], w[1], w[2], w[3]);
+      }
+    } else {
+      const SmemArray<KeyT> dst(run + lane * KPL);
+#pragma unroll
+      for (int r = 0; r < KPL; ++r) dst.put(r, x[r]);
+    }
     if constexpr (PAD > 0) {
       for (int j = lane; j < PAD; j += 32) run[Geo::WARP_RUN + j] = sentinel_key<KeyT>();
     }
