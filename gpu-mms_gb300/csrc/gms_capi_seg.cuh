@@ -30,6 +30,7 @@ struct SegJob {
 template <class Eng, class K>
 int seg_prepare(const std::vector<int64_t>& off, int64_t nseg, const gms::Tune& t, SegJob* job) {
   job->plan = gms::seg_plan(off.data(), nseg, Eng::seg_geom(t));
+  if (job->plan.too_long) return set_error(GMS_ERR_TOO_LARGE, "an array of the batch is longer than 2^31 - 1 keys");
   if (!job->plan.ok) return set_error(GMS_ERR_INVALID, "tuning too fine for this batch (sample recursion too deep)");
   job->blob = gms::seg_blob_layout(job->plan);
   job->ws_bytes = gms::ws_bytes_for<K>(gms::seg_ws_layout(job->plan), t.k);

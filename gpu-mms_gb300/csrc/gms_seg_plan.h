@@ -67,6 +67,7 @@ struct SegPlanH {
   std::vector<int> rounds;      // level index of data rounds 1 .. rounds_max
   std::vector<SegLevelH> levels;
   bool ok = true;
+  bool too_long = false;  // an array longer than 2^31 - 1 keys (run lengths are 32-bit): no plan
   // scratch sizes in entries, as WsLayout: data-level block samples, gathered
   // samples and merged samples per level, boundary rows per level
   int64_t s1 = 0;
@@ -158,6 +159,13 @@ inline int seg_add_level(SegPlanH& P, const SegGeom& G, std::vector<SegGroupH> g
 inline SegPlanH seg_plan(const int64_t* off, int64_t nseg, const SegGeom& G) {
   SegPlanH P;
   P.n = nseg > 0 ? off[nseg] : 0;
+  for (int64_t s = 0; s < nseg; ++s) {
+    if (off[s + 1] - off[s] > (int64_t)0x7fffffff) {
+      P.ok = false;
+      P.too_long = true;
+      return P;
+    }
+  }
   const int64_t k = G.k;
   std::vector<int> R((size_t)nseg, 0);
   std::vector<int64_t> first((size_t)nseg, 0), units((size_t)nseg, 0);

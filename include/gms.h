@@ -199,8 +199,9 @@ int gms_find_partitions_i32(const int32_t* task, int64_t size, int k, int64_t ta
  * merge round, larger ones in rounds bounded to the array.  The call reads
  * the offsets back to plan the batch (it waits for `stream` to reach them),
  * then enqueues the sort asynchronously.  Offsets that do not rise from 0 to
- * n are GMS_ERR_INVALID.  Scratch: about n keys (+ payload) beyond a plain
- * sort's, from the per-stream cache.
+ * n are GMS_ERR_INVALID; an array longer than 2^31 - 1 keys is
+ * GMS_ERR_TOO_LARGE (sort it with a plain call).  Scratch: about n keys
+ * (+ payload) beyond a plain sort's, from the per-stream cache.
  *
  * No counterpart in the reference: GPU-MMS sorts one array per
  * multimergesort call (src/multimergesort.hxx:56-141), each running the
@@ -315,10 +316,10 @@ int gms_workspace_status(void* workspace, void* stream, int* status_out);
  *   bit 1 (2) = a tile boundary lay outside its run;
  *   bit 2 (4) = a bulk copy into shared memory did not complete within the
  *               spin limit of its wait, and its tile was skipped (any sort,
- *               merge round or tile sort);
- *   bit 3 (8) = a batched sort's offsets were not monotone within [0, n].
- * Bits 0-2 mean the result is wrong (never expected); bit 3 means the caller's
- * offsets were bad.  Sorts with a caller-provided workspace report in that
+ *               merge round or tile sort).
+ * Any bit set means the result is wrong (never expected).  (A batched sort's
+ * offsets are checked on the host before anything is launched: bad offsets
+ * are the call's GMS_ERR_INVALID.)  Sorts with a caller-provided workspace report in that
  * workspace (gms_workspace_status), the allocation-free sort in its static
  * array (gms_noalloc_status).
  * No reference counterpart (the reference reports nothing from its kernels). */

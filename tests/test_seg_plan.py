@@ -235,3 +235,14 @@ def test_plan_edge_batches(plan_exe):
         for ln in lens:
             off.append(off[-1] + ln)
         check_plan(run_plan(plan_exe, geom, off), off, geom)
+
+
+def test_plan_refuses_an_array_past_int32(plan_exe):
+    """Run lengths are 32-bit in the plan's device arrays: an array of 2^31
+    keys gets no plan (the C ABI reports GMS_ERR_TOO_LARGE), one of 2^31 - 1
+    keys in a batch is planned."""
+    geom = (8192, 8928, 8432, 8704, 8432, 32, 32)
+    base, capd, capwd, capi, capwi, k, b = geom
+    inp = f"{base} {capd} {capwd} {capi} {capwi} {k} {b} 2\n0 5 {5 + (1 << 31)}\n"
+    out = subprocess.run([plan_exe], input=inp, capture_output=True, text=True, check=True).stdout.split("\n")
+    assert out[0].split()[:3] == ["plan", "0", "0"]
