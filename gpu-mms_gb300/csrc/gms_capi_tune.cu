@@ -241,14 +241,25 @@ gms::Tune current_tune() {
 }
 
 // Built-in tuning of a class when neither gms_set_tune nor the autotuned
-// table says otherwise (timed on GB300, 2^27 keys): sorts with a payload
-// merge faster with persistent CTAs that stage the next tile while storing
-// the current one (float32 + int32 -2%, uint64 + int32 -4%); keys-only sorts
-// do not (+1%).
-gms::Tune builtin_tune(int dtype, int kv) {
-  (void)dtype;
+// table says otherwise (timed on GB300).
+//   Staging (2^27 keys): sorts with a payload and sorts of 64-bit keys merge
+//   faster with persistent CTAs that stage the next tile while storing the
+//   current one (float32 + int32 -2%, uint64 + int32 -4%, uint64 keys alone
+//   -2%: 7.90 against 8.08 ms); sorts of 32-bit keys alone do not (+1%).
+//   Fan-in (keys-only sorts): gms_engines::balanced_fan_in.  A fan-in of 32
+//   on 2048 base runs (int32, 2^24 keys) would spend its third round merging
+//   2 runs; 16 gives three even rounds: 0.49 against 0.60 ms (int32 2^20:
+//   0.109 against 0.124; uint64 2^24: 0.92 against 1.06, 2^18: fan-in 8,
+//   0.081 against 0.118 ms), while 2^22, 2^26 and 2^28 keep 32 (their
+//   rounds are even).
+gms::Tune builtin_tune(int dtype, int kv, int64_t n) {
   gms::Tune t;
-  if (kv) t.bulk_copy = 3;
+  if (kv || dtype >= 3) t.bulk_copy = 3;  // dtypes 3-5: int64, uint64, float64
+  if (!kv) {
+    const int64_t base = dtype >= 3 ? (int64_t)KeysEngine<uint64_t, gms::IdentityCodec<uint64_t>>::BASE_TILE
+                                    : (int64_t)KeysEngine<uint32_t, gms::IdentityCodec<uint32_t>>::BASE_TILE;
+    t = gms_engines::balanced_fan_in(n, base, t);
+  }
   return t;
 }
 
@@ -260,7 +271,7 @@ gms::Tune tune_for(int dtype, int kv, int64_t n) {
   const int c = size_class(n);
   for (const TuneEntry& e : g_table)
     if (e.dtype == dtype && e.kv == kv && e.cls == c) return e.t;
-  return builtin_tune(dtype, kv);
+  return builtin_tune(dtype, kv, n);
 }
 
 }  // namespace gms_capi

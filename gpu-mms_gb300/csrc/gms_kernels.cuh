@@ -541,15 +541,15 @@ __global__ void __launch_bounds__(NT) base_warp_kernel(TileArgs<KeyT, NoVal> a0)
     KeyT* run = k0 + warp * (Geo::WARP_RUN + PAD);
     constexpr int KPC = 16 / (int)sizeof(KeyT);  // keys per 16-byte chunk
     constexpr int NC = KPL / KPC;                // chunks per lane
-    if constexpr (NC == 8 && ((Geo::WARP_RUN + PAD) * sizeof(KeyT)) % 16 == 0) {
-      // A lane's run is 128 bytes, so the same store of every lane would hit
-      // the same banks.  Lane l writes its chunk c ^ (l & 7) at step c
-      // instead: the eight lanes of a quarter-warp then write eight
+    if constexpr (NC >= 8 && NC % 8 == 0 && ((Geo::WARP_RUN + PAD) * sizeof(KeyT)) % 16 == 0) {
+      // A lane's run is a multiple of 128 bytes, so the same store of every
+      // lane would hit the same banks.  Lane l writes its chunk c ^ (l & 7)
+      // at step c instead: the eight lanes of a quarter-warp then write eight
       // different bank groups (conflict-free 16-byte stores).  The chunks
       // are XOR-permuted in registers first (three conditional swaps).
       const int t = lane & 7;
 #pragma unroll
-      for (int b = 1; b < NC; b <<= 1) {
+      for (int b = 1; b < 8; b <<= 1) {
         const bool sw = (t & b) != 0;
 #pragma unroll
         for (int c = 0; c < NC; ++c) {
@@ -563,7 +563,8 @@ __global__ void __launch_bounds__(NT) base_warp_kernel(TileArgs<KeyT, NoVal> a0)
           }
         }
       }
-      const uint32_t base = static_cast<uint32_t>(__cvta_generic_to_shared(run)) + 128u * (uint32_t)lane;
+      const uint32_t base =
+          static_cast<uint32_t>(__cvta_generic_to_shared(run)) + (uint32_t)(KPL * sizeof(KeyT)) * (uint32_t)lane;
 #pragma unroll
       for (int c = 0; c < NC; ++c) {
         uint32_t w[4];

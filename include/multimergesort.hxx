@@ -117,12 +117,15 @@ inline void* scratch(size_t bytes, cudaError_t* err) {
   return slot->ptr;
 }
 
-// One sort through engine Eng on keys of stored type KT.
-template <class Eng, class KT>
+// One sort through engine Eng on keys of stored type KT.  BY_SIZE: the
+// fan-in and sample block follow N (gms_engines::balanced_fan_in), as in the
+// prebuilt library, unless the caller fixed GMS_K / GMS_SAMPLE_B.
+template <class Eng, class KT, bool BY_SIZE = false>
 cudaError_t sort_with(KT* input, KT* output, int N) {
   gms::Tune t;
   t.k = GMS_K;
   t.sample_b = GMS_SAMPLE_B;
+  if constexpr (BY_SIZE) t = gms_engines::balanced_fan_in((int64_t)N, Eng::BASE_TILE, t);
   const gms::WsLayout l = Eng::plan((int64_t)N, t);
   if (!l.ok) return cudaErrorInvalidValue;
   cudaError_t e = cudaSuccess;
@@ -151,8 +154,13 @@ T* run(T* input, T* output, int N) {
   if constexpr (fast_keys<T, f>()) {
     using BK = gms_engines::BuiltinKey<T>;
     using KT = typename BK::Stored;
-    e = sort_with<gms_engines::KeysEngine<KT, typename BK::Codec>, KT>(reinterpret_cast<KT*>(input),
-                                                                      reinterpret_cast<KT*>(output), N);
+#ifdef GMS_FAN_IN_BY_SIZE
+    constexpr bool by_size = true;
+#else
+    constexpr bool by_size = false;
+#endif
+    e = sort_with<gms_engines::KeysEngine<KT, typename BK::Codec>, KT, by_size>(reinterpret_cast<KT*>(input),
+                                                                               reinterpret_cast<KT*>(output), N);
   } else {
     e = sort_with<DropinEngine<T, f>, T>(input, output, N);
   }

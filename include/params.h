@@ -14,6 +14,11 @@
 /* ---- GB300 engine ---- */
 #ifndef GMS_K
 #define GMS_K 32        /* fan-in of a merge round (2..32)                     */
+/* neither given: built-in integer keys under the default order take the
+ * fan-in that balances the rounds for each N (see sort_with) */
+#ifndef GMS_SAMPLE_B
+#define GMS_FAN_IN_BY_SIZE 1
+#endif
 #endif
 #ifndef GMS_SAMPLE_B
 #define GMS_SAMPLE_B 32 /* block size of the forecast sample that cuts tiles    */

@@ -15,6 +15,7 @@ pytestmark = pytest.mark.gpu
 
 DEFAULT = {"k": 32, "sample_b": 32, "bulk_copy": 1}
 DEFAULT_KV = {"k": 32, "sample_b": 32, "bulk_copy": 3}  # built-in for sorts with a payload
+DEFAULT_64 = DEFAULT_KV  # and for sorts of 64-bit keys
 
 
 @pytest.fixture
@@ -94,7 +95,7 @@ def test_cache_round_trip(gms, clean, tmp_path):
     assert len(doc["entries"]) == 2
     lib = clean
     assert lib.gms_autotune_clear() == 0
-    assert gms.tune_for("int64", 1 << 21) == DEFAULT
+    assert gms.tune_for("int64", 1 << 21) == DEFAULT_64
     gms.autotune_load(path)
     assert sorted(map(json.dumps, gms.autotune_table())) == sorted(map(json.dumps, table))
     # another GPU model's cache is refused and leaves the table as it was

@@ -56,6 +56,30 @@ def test_tuning_state(lib):
     assert get_tune(lib) == (32, 32, 1)
 
 
+def test_builtin_fan_in_balances_the_rounds(lib):
+    """Keys-only sorts take the fewest rounds a fan-in of at most 32 allows
+    and the smallest power-of-two fan-in that keeps that many rounds (block
+    sample 64 below a fan-in of 32); key/value sorts keep 32 / 32."""
+    lib.gms_clear_tune()
+    # int32: base runs of 8192 keys
+    assert tune_for(lib, 0, 0, 1 << 13) == (32, 32, 1)  # one base tile: no round
+    assert tune_for(lib, 0, 0, 1 << 18) == (32, 32, 1)  # 32 runs: one round of 32
+    assert tune_for(lib, 0, 0, 1 << 20) == (16, 64, 1)  # 128 runs: two rounds of 16 (not 32 + 4)
+    assert tune_for(lib, 0, 0, 1 << 22) == (32, 32, 1)  # 512 runs: two rounds of 32
+    assert tune_for(lib, 0, 0, 1 << 24) == (16, 64, 1)  # 2048 runs: three rounds of 16 (not 32, 32, 2)
+    assert tune_for(lib, 0, 0, (1 << 24) + 1) == (16, 64, 1)  # 2049 runs: 16^3 = 4096 still covers them
+    assert tune_for(lib, 1, 0, 1 << 26) == (32, 32, 1)
+    assert tune_for(lib, 2, 0, 1 << 28) == (32, 32, 1)
+    # 64-bit keys: base runs of 4096 keys, persistent staging
+    assert tune_for(lib, 4, 0, 1 << 18) == (8, 64, 3)   # 64 runs: two rounds of 8
+    assert tune_for(lib, 3, 0, 1 << 24) == (16, 64, 3)
+    assert tune_for(lib, 5, 0, 1 << 22) == (32, 32, 3)
+    # payload sorts keep the defaults
+    assert tune_for(lib, 2, 1, 1 << 24) == (32, 32, 3)
+    assert tune_for(lib, 4, 1, 1 << 20) == (32, 32, 3)
+    assert lib.gms_rounds(0, 0, 1 << 24) == 3
+
+
 def test_rounds_follow_the_fan_in(lib):
     try:
         assert lib.gms_rounds(0, 0, 1 << 28) == 3  # 8192 * 32^3 = 2^28
