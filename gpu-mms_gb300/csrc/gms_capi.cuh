@@ -43,6 +43,10 @@ void* cache_get(int tag, size_t bytes, cudaStream_t st, int* status);
 // one; else the defaults gms::Tune{}.
 gms::Tune current_tune();
 gms::Tune tune_for(int dtype, int kv, int64_t n);
+// The tuning of a batch of arrays (n keys in all, the longest `longest`
+// keys): an explicit or autotuned tuning of n's size class, else the
+// built-in one for the longest array (its rounds are the batch's rounds).
+gms::Tune tune_for_batch(int dtype, int kv, int64_t n, int64_t longest);
 inline gms::Tune default_tune() { return current_tune(); }
 
 // Frees the host-sort pipelines (streams, events, staging buffers).

@@ -2,6 +2,7 @@
 // a sort.  The batched entry points themselves sit with the plain sorts of
 // their key type (gms_capi_k32.cu, gms_capi_k64.cu, gms_capi_kv.cu), whose
 // kernels they share.
+#include <algorithm>
 #include <new>
 #include <vector>
 
@@ -116,7 +117,9 @@ int gms_graph_create_segmented_i32(int32_t* in, int32_t* out, int64_t n, const i
   std::vector<int64_t> h;
   int status = read_offsets(offsets, nseg, n, st, &h);
   if (status != GMS_OK) return status;
-  const gms::Tune t = tune_for(0, 0, n);
+  int64_t longest = 0;
+  for (int64_t s = 0; s < nseg; ++s) longest = std::max(longest, h[(size_t)(s + 1)] - h[(size_t)s]);
+  const gms::Tune t = tune_for_batch(0, 0, n, longest);
   SegJob* job = new (std::nothrow) SegJob;
   if (!job) return set_error(GMS_ERR_NOMEM, "graph plan");
   status = seg_prepare_i32(h, nseg, t, job);

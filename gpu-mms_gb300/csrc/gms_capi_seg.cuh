@@ -8,6 +8,7 @@
 // call (GPU-MMS src/multimergesort.hxx:56-141).
 #pragma once
 
+#include <algorithm>
 #include <vector>
 
 #include "gms_capi.cuh"
@@ -97,7 +98,9 @@ int run_segmented(const K* in, const V* vin, K* out, V* vout, int64_t n, const i
   std::vector<int64_t> h;
   int status = read_offsets(off, nseg, n, st, &h);
   if (status != GMS_OK) return status;
-  const gms::Tune t = tune_for(dtype, kv ? 1 : 0, n);
+  int64_t longest = 0;
+  for (int64_t s = 0; s < nseg; ++s) longest = std::max(longest, h[(size_t)(s + 1)] - h[(size_t)s]);
+  const gms::Tune t = tune_for_batch(dtype, kv ? 1 : 0, n, longest);
   SegJob job;
   status = seg_prepare<Eng, K>(h, nseg, t, &job);
   if (status != GMS_OK) return status;

@@ -246,12 +246,13 @@ gms::Tune current_tune() {
 //   faster with persistent CTAs that stage the next tile while storing the
 //   current one (float32 + int32 -2%, uint64 + int32 -4%, uint64 keys alone
 //   -2%: 7.90 against 8.08 ms); sorts of 32-bit keys alone do not (+1%).
-//   Fan-in (keys-only sorts): gms_engines::balanced_fan_in.  A fan-in of 32
-//   on 2048 base runs (int32, 2^24 keys) would spend its third round merging
-//   2 runs; 16 gives three even rounds: 0.49 against 0.60 ms (int32 2^20:
-//   0.109 against 0.124; uint64 2^24: 0.92 against 1.06, 2^18: fan-in 8,
-//   0.081 against 0.118 ms), while 2^22, 2^26 and 2^28 keep 32 (their
-//   rounds are even).
+//   Fan-in: gms_engines::balanced_fan_in.  A fan-in of 32 on 2048 base runs
+//   (int32, 2^24 keys) would spend its third round merging 2 runs; 16 gives
+//   three even rounds: 0.49 against 0.60 ms (int32 2^20: 0.109 against
+//   0.124; uint64 2^24: 0.92 against 1.06, 2^18: fan-in 8, 0.081 against
+//   0.118 ms; float32 + int32 2^24: fan-in 16, 0.88 against 1.01, 2^18:
+//   fan-in 8, 0.077 against 0.106 ms), while 2^22, 2^26 and 2^28 keep 32
+//   (their rounds are even).
 gms::Tune builtin_tune(int dtype, int kv, int64_t n) {
   gms::Tune t;
   if (kv || dtype >= 3) t.bulk_copy = 3;  // dtypes 3-5: int64, uint64, float64
@@ -259,11 +260,15 @@ gms::Tune builtin_tune(int dtype, int kv, int64_t n) {
     const int64_t base = dtype >= 3 ? (int64_t)KeysEngine<uint64_t, gms::IdentityCodec<uint64_t>>::BASE_TILE
                                     : (int64_t)KeysEngine<uint32_t, gms::IdentityCodec<uint32_t>>::BASE_TILE;
     t = gms_engines::balanced_fan_in(n, base, t);
+  } else {
+    t = gms_engines::balanced_fan_in(n, (int64_t)KvEngine<uint32_t, gms::IdentityCodec<uint32_t>>::BASE_TILE, t, 16);
   }
   return t;
 }
 
-gms::Tune tune_for(int dtype, int kv, int64_t n) {
+gms::Tune tune_for(int dtype, int kv, int64_t n) { return tune_for_batch(dtype, kv, n, n); }
+
+gms::Tune tune_for_batch(int dtype, int kv, int64_t n, int64_t longest) {
   if (t_override) return *t_override;
   autoload();
   std::lock_guard<std::mutex> g(g_tune_mu);
@@ -271,7 +276,7 @@ gms::Tune tune_for(int dtype, int kv, int64_t n) {
   const int c = size_class(n);
   for (const TuneEntry& e : g_table)
     if (e.dtype == dtype && e.kv == kv && e.cls == c) return e.t;
-  return builtin_tune(dtype, kv, n);
+  return builtin_tune(dtype, kv, longest);
 }
 
 }  // namespace gms_capi

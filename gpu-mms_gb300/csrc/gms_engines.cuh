@@ -45,20 +45,22 @@ template <class Key, class Codec>
 using KvEngine =
     gms::Engine<Key, int32_t, gms::KeyLess, Codec, true, 256, 17, gms::MergeGeo<288, 15, 1>, IndexGeo>;
 
-// Fan-in of a keys-only sort of n keys over base-case runs of `base` keys:
-// a round costs about the same whatever its fan-in, so the sort takes the
-// fewest rounds a fan-in of at most 32 allows, R = ceil(log2(runs) / 5), with
-// the smallest power-of-two fan-in that still needs only R rounds,
-// 2^ceil(log2(runs) / R), and a block sample of 64 keys when that fan-in is
-// below 32 (int32 2^24: fan-in 16 in three even rounds, 0.49 ms, against 32,
-// 32, 2 with a fan-in of 32, 0.60 ms on GB300).  Other tunables stay as in t.
-inline gms::Tune balanced_fan_in(int64_t n, int64_t base, gms::Tune t) {
+// Fan-in of a sort of n keys over base-case runs of `base` keys: a round
+// costs about the same whatever its fan-in, so the sort takes the fewest
+// rounds a fan-in of at most 32 allows, R = ceil(log2(runs) / 5), with the
+// smallest power-of-two fan-in that still needs only R rounds,
+// 2^ceil(log2(runs) / R) (int32 2^24: fan-in 16 in three even rounds, 0.49
+// ms, against 32, 32, 2 with a fan-in of 32, 0.60 ms on GB300), and a block
+// sample of 64 keys when that fan-in is below `wide_below` (keys-only sorts:
+// 32; sorts with a payload, whose smaller tiles lose more to the coarser
+// sample: 16).  Other tunables stay as in t.
+inline gms::Tune balanced_fan_in(int64_t n, int64_t base, gms::Tune t, int wide_below = 32) {
   int lg = 0;  // log2 of the base-case runs, rounded up
   while ((base << lg) < n && lg < 40) ++lg;
   const int rounds = (lg + 4) / 5;
   if (rounds > 0) {
     t.k = 1 << ((lg + rounds - 1) / rounds);
-    t.sample_b = t.k < 32 ? 64 : 32;
+    t.sample_b = t.k < wide_below ? 64 : 32;
   }
   return t;
 }

@@ -235,9 +235,13 @@ void dispatcher_main(gms_server* s) {
     if (batch) {
       // plan the batch from its sizes, here on the host
       std::vector<int64_t> off(ids.size() + 1, 0);
-      for (size_t i = 0; i < ids.size(); ++i) off[i + 1] = off[i] + s->reqs[ids[i]].n;
+      int64_t longest = 0;
+      for (size_t i = 0; i < ids.size(); ++i) {
+        off[i + 1] = off[i] + s->reqs[ids[i]].n;
+        longest = std::max(longest, s->reqs[ids[i]].n);
+      }
       const int kind = s->reqs[ids[0]].kind;
-      it.tune = tune_for(kind == 0 ? 0 : 4, kind, off.back());
+      it.tune = tune_for_batch(kind == 0 ? 0 : 4, kind, off.back(), longest);
       it.job.reset(new (std::nothrow) SegJob);
       int st2 = it.job ? (kind == 0 ? seg_prepare_i32(off, (int64_t)ids.size(), it.tune, it.job.get())
                                     : seg_prepare_kv_u64(off, (int64_t)ids.size(), it.tune, it.job.get()))

@@ -74,9 +74,12 @@ def test_builtin_fan_in_balances_the_rounds(lib):
     assert tune_for(lib, 4, 0, 1 << 18) == (8, 64, 3)   # 64 runs: two rounds of 8
     assert tune_for(lib, 3, 0, 1 << 24) == (16, 64, 3)
     assert tune_for(lib, 5, 0, 1 << 22) == (32, 32, 3)
-    # payload sorts keep the defaults
-    assert tune_for(lib, 2, 1, 1 << 24) == (32, 32, 3)
-    assert tune_for(lib, 4, 1, 1 << 20) == (32, 32, 3)
+    # payload sorts: base runs of 4352 keys, block sample 64 only below fan-in 16
+    assert tune_for(lib, 2, 1, 1 << 18) == (8, 64, 3)    # 61 runs: two rounds of 8
+    assert tune_for(lib, 4, 1, 1 << 20) == (16, 32, 3)   # 241 runs: two rounds of 16
+    assert tune_for(lib, 2, 1, 1 << 22) == (32, 32, 3)   # 964 runs: two rounds of 32
+    assert tune_for(lib, 4, 1, 1 << 24) == (16, 32, 3)   # 3856 runs: three rounds of 16
+    assert tune_for(lib, 2, 1, 1 << 27) == (32, 32, 3)
     assert lib.gms_rounds(0, 0, 1 << 24) == 3
 
 
