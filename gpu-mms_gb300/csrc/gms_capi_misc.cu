@@ -165,6 +165,15 @@ const char* gms_status_string(int s) {
 
 const char* gms_last_error(void) { return g_last_error.c_str(); }
 
+int gms_set_pdl(int on) {
+  clear_error();
+  if (on != 0 && on != 1) return set_error(GMS_ERR_INVALID, "gms_set_pdl takes 0 or 1");
+  gms::pdl_enabled().store(on, std::memory_order_relaxed);
+  return GMS_OK;
+}
+
+int gms_get_pdl(void) { return gms::pdl_enabled().load(std::memory_order_relaxed); }
+
 void gms_release_workspaces(void) {
   release_host_pipes();
   release_noalloc_symbols();

@@ -23,6 +23,17 @@
 namespace gms {
 
 // ---------------------------------------------------------------------------
+// Programmatic dependent launch.  The engine launches its kernels with
+// programmatic stream serialization: a kernel's launch is set up while the
+// previous kernel of the stream runs, and its CTAs are scheduled as that
+// kernel's CTAs exit (no kernel ever triggers its dependents early -- CTAs
+// that wait for the rest of a long last wave only take SM slots).  Every such
+// kernel calls pdl_wait() before it touches global memory; the wait returns
+// once the previous kernel has completed and its writes are visible.  Without
+// a programmatic dependency it is a no-op.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+// ---------------------------------------------------------------------------
 // Payload marker for keys-only sorts.
 struct NoVal {};
 

@@ -147,6 +147,7 @@ struct EncCmp {
 template <class KeyT, class V, class Cmp, class Codec, int MODE, bool STABLE, int NT, int ITEMS>
 __global__ void __launch_bounds__(NT, (MODE == MODE_BASE && sizeof(KeyT) == 4 && !HasVal<V>::value) ? 3 : 1)
     tile_kernel(TileArgs<KeyT, V> a0) {
+  pdl_wait();
   TileArgs<KeyT, V> a = a0;
   const GroupDesc* gd = a.grp ? a.grp + blockIdx.x : nullptr;
   if (gd) use_group(a, gd->flags);
@@ -463,6 +464,7 @@ struct BaseWarpSmem {
 // group (tile) t.
 template <class KeyT, class Cmp, class Codec, int NT, int KPL, int ITEMS_M, int NSB = 2>
 __global__ void __launch_bounds__(NT) base_warp_kernel(TileArgs<KeyT, NoVal> a0) {
+  pdl_wait();
   TileArgs<KeyT, NoVal> a = a0;
   const GroupDesc* gd = a.grp ? a.grp + blockIdx.x : nullptr;
   if (gd) use_group(a, gd->flags);
@@ -720,6 +722,7 @@ using MergeLayoutOf =
 template <class KeyT, class V, class Cmp, class Codec, int NT, int ITEMS, int NS, int COPY = 1, bool PERSIST = false>
 __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, int64_t total_tiles) {
   static_assert(!PERSIST || COPY == 1, "persistent tiles stage with bulk copies");
+  pdl_wait();
   constexpr int CAP = NT * ITEMS;                        // shared-memory buffers
   constexpr int TILE_MAX = WindowCap<NT, ITEMS>::value;  // keys a tile may hold
   constexpr bool kHasVal = HasVal<V>::value;
@@ -1205,6 +1208,7 @@ __global__ void __launch_bounds__(256) splitter_kernel(const KeyT* __restrict__ 
                                                         int enc, const GroupDesc* __restrict__ grp,
                                                         const int32_t* __restrict__ row_grp,
                                                         const KeyT* __restrict__ data2, int direct) {
+  pdl_wait();
   const Cmp cmp;
   const int lane = threadIdx.x & 31;
   const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -1303,6 +1307,7 @@ template <class KeyT, class Codec>
 __global__ void gather_sample_kernel(const KeyT* __restrict__ in, KeyT* __restrict__ out, int64_t n_in, int64_t in_run,
                                      int64_t out_run, int b_step, int64_t n_out_slots, int enc,
                                      const int32_t* __restrict__ run_len) {
+  pdl_wait();
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n_out_slots) return;
   const int64_t r = t / out_run;

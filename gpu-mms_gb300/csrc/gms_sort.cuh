@@ -21,6 +21,7 @@
 #pragma once
 
 #include <algorithm>
+#include <atomic>
 #include <cstdint>
 #include <cstring>
 #include <mutex>
@@ -61,6 +62,13 @@ inline void hook_before(int kc, cudaStream_t st) {
 }
 inline void hook_after(int kc, cudaStream_t st) {
   if (g_hooks) g_hooks->after(kc, st);
+}
+
+// Programmatic dependent launch of the engine's kernels (process-wide switch,
+// on by default; the C ABI's gms_set_pdl sets it).
+inline std::atomic<int>& pdl_enabled() {
+  static std::atomic<int> on{1};
+  return on;
 }
 
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
@@ -439,6 +447,26 @@ struct Engine {
   }
 
   // ---------------- launches ----------------
+  // Every engine kernel goes out with programmatic stream serialization while
+  // pdl_enabled() (its launch is set up while the previous kernel runs; the
+  // kernel waits in pdl_wait() for that kernel's results).
+  template <class... KArgs, class... Args>
+  static cudaError_t launch_kernel(void (*kern)(KArgs...), int64_t grid, int block, size_t smem, cudaStream_t st,
+                                   Args... args) {
+    if (grid <= 0 || grid > 0x7fffffff) return cudaErrorInvalidConfiguration;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl_enabled().load(std::memory_order_relaxed) ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kern, args...);
+  }
+
   template <int MODE, class VV>
   static cudaError_t launch_tile(const TileArgs<KeyT, VV>& a, int64_t grid, cudaStream_t st, int level = 0) {
     if (grid <= 0) return cudaSuccess;
@@ -452,8 +480,7 @@ struct Engine {
     if (grid > 0x7fffffff) return cudaErrorInvalidConfiguration;
     const int kc = (MODE == MODE_BASE) ? KC_BASE : (level == 0 ? KC_MERGE : KC_SAMPLE_MERGE);
     hook_before(kc, st);
-    kern<<<(unsigned)grid, kNT, smem, st>>>(a);
-    e = cudaGetLastError();
+    e = launch_kernel(kern, grid, kNT, smem, st, a);
     hook_after(kc, st);
     return e;
   }
@@ -468,8 +495,7 @@ struct Engine {
       cudaError_t e = ensure_smem((const void*)kern, smem);
       if (e != cudaSuccess) return e;
       hook_before(KC_BASE, st);
-      kern<<<(unsigned)grid, kNTB, smem, st>>>(a);
-      e = cudaGetLastError();
+      e = launch_kernel(kern, grid, kNTB, smem, st, a);
       hook_after(KC_BASE, st);
       return e;
     } else {
@@ -507,8 +533,7 @@ struct Engine {
     }
     const int kc = level == 0 ? KC_MERGE : KC_SAMPLE_MERGE;
     hook_before(kc, st);
-    kern<<<(unsigned)grid, GG::NT, smem, st>>>(a, total_tiles);
-    e = cudaGetLastError();
+    e = launch_kernel(kern, grid, GG::NT, smem, st, a, total_tiles);
     hook_after(kc, st);
     return e;
   }
@@ -568,9 +593,8 @@ struct Engine {
       KeyT* g = w.s[level + 1];
       const int64_t slots = runs * Ls;
       hook_before(KC_GATHER, st);
-      gather_sample_kernel<KeyT, Codec><<<(unsigned)ceil_div(slots, 256), 256, 0, st>>>(
-          in, g, n, L, Ls, sb, slots, enc, sl ? sl->run_len : nullptr);
-      e = cudaGetLastError();
+      e = launch_kernel(gather_sample_kernel<KeyT, Codec>, ceil_div(slots, 256), 256, 0, st, in, g, n, L, Ls, sb,
+                        slots, enc, sl ? sl->run_len : nullptr);
       hook_after(KC_GATHER, st);
       if (e != cudaSuccess) return e;
       S = g;
@@ -587,10 +611,10 @@ struct Engine {
     {
       const int64_t threads = rows * 32;
       hook_before(KC_SPLIT, st);
-      splitter_kernel<KeyT, Cmp, Codec><<<(unsigned)ceil_div(threads, 256), 256, 0, st>>>(
-          in, S, w.fk[level + 1], w.fi[level + 1], n, L, k, Ls, sb, G, tiles_full, tiles_last, groups, w.desc[level],
-          w.doff[level], enc, sl ? sl->grp : nullptr, sl ? sl->row_grp : nullptr, in2, t.split);
-      e = cudaGetLastError();
+      e = launch_kernel(splitter_kernel<KeyT, Cmp, Codec>, ceil_div(threads, 256), 256, 0, st, in, S,
+                        (const KeyT*)w.fk[level + 1], (const uint32_t*)w.fi[level + 1], n, L, k, Ls, sb, G, tiles_full,
+                        tiles_last, groups, w.desc[level], w.doff[level], enc, sl ? sl->grp : nullptr,
+                        sl ? sl->row_grp : nullptr, in2, t.split);
       hook_after(KC_SPLIT, st);
       if (e != cudaSuccess) return e;
     }

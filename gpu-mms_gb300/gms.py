@@ -173,6 +173,8 @@ SIGNATURES = {
     "gms_graph_create_sort_i32": (_i32, [_vp, _vp, _i64, _vp, ctypes.POINTER(_vp)]),
     "gms_graph_create_segmented_i32": (_i32, [_vp, _vp, _i64, _vp, _i64, _vp, ctypes.POINTER(_vp)]),
     "gms_graph_launch": (_i32, [_vp, _vp]),
+    "gms_set_pdl": (_i32, [_i32]),
+    "gms_get_pdl": (_i32, []),
     "gms_server_create": (_i32, [_sz, _i32, _i64, _i64, ctypes.POINTER(_vp)]),
     "gms_server_submit": (_i32, [_vp, _i32, _vp, _vp, _vp, _vp, _i64, ctypes.POINTER(ctypes.c_uint64)]),
     "gms_server_wait": (_i32, [_vp, ctypes.c_uint64, ctypes.POINTER(ctypes.c_double)]),

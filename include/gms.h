@@ -295,6 +295,16 @@ size_t gms_workspace_bytes(int dtype, int kv, int64_t n);
 int gms_reserve(int dtype, int kv, int64_t n, void* stream);
 void gms_release_workspaces(void);
 
+/* Programmatic dependent launch (process-wide, on by default): the sort
+ * kernels go out with programmatic stream serialization, so each kernel's
+ * launch is set up while the previous one runs and its CTAs start as that
+ * kernel's CTAs exit, waiting on the device for its results (shorter gaps
+ * between the kernels: int32 2^20 keys 0.095 instead of 0.116 ms, 2^24 0.457
+ * instead of 0.490 ms on GB300).  gms_set_pdl(0) launches them in plain stream
+ * order.  No counterpart in the reference, whose kernels launch with <<<>>>. */
+int gms_set_pdl(int on);
+int gms_get_pdl(void);
+
 /* Explicit workspace (for serving layers that own their memory): one sort of
  * `dtype`/`kv` (codes above; vals NULL when kv = 0) that uses `workspace`, a
  * 256-byte-aligned device buffer of at least gms_workspace_bytes(dtype, kv, n)

@@ -94,6 +94,19 @@ def test_rounds_follow_the_fan_in(lib):
         lib.gms_clear_tune()
 
 
+def test_pdl_switch(lib):
+    """Programmatic dependent launch is on by default and switchable."""
+    try:
+        assert lib.gms_get_pdl() == 1
+        assert lib.gms_set_pdl(0) == GMS_OK
+        assert lib.gms_get_pdl() == 0
+        assert lib.gms_set_pdl(2) == GMS_ERR_INVALID
+        assert lib.gms_get_pdl() == 0
+    finally:
+        lib.gms_set_pdl(1)
+    assert lib.gms_get_pdl() == 1
+
+
 def test_argument_checks_before_device_work(lib):
     vp = ctypes.c_void_p
     assert lib.gms_sort_ws(9, 0, None, None, None, None, 10, None, 0, None) == GMS_ERR_INVALID
