@@ -219,6 +219,39 @@ def test_deterministic_repeats(gms, oracle):
         assert_same(gpu_sort(gms, a), first)
 
 
+def test_programmatic_launch_on_off_and_two_streams(gms, oracle):
+    """Sorts launched with programmatic dependent launch (the default) and in
+    plain stream order give the oracle's result, also while two streams sort
+    at the same time (each stream's kernels wait only for their own
+    predecessors)."""
+    lib = gms.load()
+    sizes = (300_007, 2_000_003, 9_000_001)
+    inputs = [oracle.gen_i32(n, d, 40 + d) for d, n in enumerate(sizes)]
+    wants = [oracle.sort(a) for a in inputs]
+    try:
+        for pdl in (1, 0):
+            assert lib.gms_set_pdl(pdl) == 0
+            for a, want in zip(inputs, wants):
+                assert_same(gpu_sort(gms, a), want, f"pdl={pdl} n={a.size}")
+        assert lib.gms_set_pdl(1) == 0
+        streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+        tins = [to_dev(a) for a in inputs[1:]]
+        touts = [torch.empty_like(t) for t in tins]
+        torch.cuda.synchronize()
+        for rep in range(3):
+            for s, tin, tout in zip(streams, tins, touts):
+                with torch.cuda.stream(s):
+                    tin_c = tin.clone()
+                    st = lib.gms_sort_i32(tin_c.data_ptr(), tout.data_ptr(), tin.numel(), 0,
+                                          ctypes.c_void_p(s.cuda_stream))
+                    assert st == 0, lib.gms_last_error()
+            torch.cuda.synchronize()
+            for tout, want in zip(touts, wants[1:]):
+                assert_same(from_dev(tout, np.int32), want, f"two streams, rep {rep}")
+    finally:
+        lib.gms_set_pdl(1)
+
+
 def test_host_entry_point(gms, oracle):
     lib = gms.load()
     a = oracle.gen_i32(1_000_003, 0, 8)
