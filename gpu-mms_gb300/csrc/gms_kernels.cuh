@@ -211,7 +211,9 @@ __global__ void __launch_bounds__(NT, (MODE == MODE_BASE && sizeof(KeyT) == 4 &&
           if ((tid & 31) == 0) *timed_out = ok ? 0 : 1;
           if (!ok) {
             if ((tid & 31) == 0 && a.err) atomicOr(a.err, DEV_COPY_TIMEOUT);
-            mbar_wait_bounded(bar, 0, kSpinLimit);  // let the copies in flight land
+            // let the copies in flight land (a second timeout returns anyway: the
+            // status bit already marks the result invalid)
+            mbar_wait_bounded(bar, 0, kSpinLimit);
           }
         }
         __syncthreads();
@@ -505,7 +507,9 @@ __global__ void __launch_bounds__(NT) base_warp_kernel(TileArgs<KeyT, NoVal> a0)
       if (lane == 0) *timed_out = ok ? 0 : 1;
       if (!ok) {
         if (lane == 0 && a.err) atomicOr(a.err, DEV_COPY_TIMEOUT);
-        mbar_wait_bounded(bar, 0, kSpinLimit);  // let the copy in flight land
+        // let the copies in flight land (a second timeout returns anyway: the
+        // status bit already marks the result invalid)
+        mbar_wait_bounded(bar, 0, kSpinLimit);
       }
     }
     __syncthreads();
@@ -1029,7 +1033,10 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
         if (lane == 0) *d.status = ok ? 0 : 1;
         if (!ok) {
           if (lane == 0 && a.err) atomicOr(a.err, DEV_COPY_TIMEOUT);
-          mbar_wait_bounded(bar, parity, kSpinLimit);  // let copies in flight land
+          // let copies in flight land; should this wait run out as well, the CTA
+          // still returns -- accepted only because the status bit already marks
+          // the sort's result as invalid
+          mbar_wait_bounded(bar, parity, kSpinLimit);
         } else {
           __syncwarp();  // lane 0's descriptor writes are visible to the warp
           pad_segments(lane, 32);
