@@ -1193,11 +1193,17 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
 // every run, merged in (key, run, block) order) is cut every G entries.  The
 // first key of block F[j*G] is boundary j.  One warp per boundary; lane k finds
 // how many keys of run k precede the boundary in the stable (key, run, index)
-// order: first by binary search over run k's block sample `samp` (small and
-// cache-resident), which brackets the answer to one block, then inside that
-// block of the run.  Between two boundaries every run contributes at most
-// (its blocks in that stretch of F + 1) blocks, so a tile holds at most
-// (G + K) * B keys.
+// order: first the number of run k's blocks whose first key precedes the
+// boundary -- which brackets the answer to one block -- then inside that block
+// of the run.  The block count is one more than the block index of run k's
+// last entry in F before position j*G: the warp scans F's index stream
+// backwards from there, 32 entries per coalesced load, until every run has
+// shown up (uniform keys: a few loads), the group's sample starts, or
+// kScanChunks loads are spent (or two loads show no other run, as in sorted
+// stretches); a run not seen by then binary-searches its block sample `samp`
+// instead.  Between two boundaries every run contributes
+// at most (its blocks in that stretch of F + 1) blocks, so a tile holds at
+// most (G + K) * B keys.
 // Segmented rounds (grp set): row r belongs to group row_grp[r]; the group's
 // runs, block samples and merged sample follow its GroupDesc, and GRP_ALT
 // groups read `data2`.
@@ -1241,6 +1247,50 @@ __global__ void __launch_bounds__(256) splitter_kernel(const KeyT* __restrict__ 
     ng = min64(L * k, n - gbase);
     run0 = g * (int64_t)k;
   }
+  // block counts from F's index stream (all lanes of the warp take part)
+  constexpr int kScanChunks = 8;  // 32-entry chunks of F a boundary scans at most
+  __shared__ int32_t scan_slot[8][32];
+  int32_t* slot = scan_slot[(threadIdx.x >> 5) & 7];
+  const bool inner = j > 0 && j < jg;
+  const int64_t fbase = run0 * sample_run_len;
+  const int64_t fpos = fbase + j * G;
+  int64_t kb = -1;
+  int64_t scan_lo = -1;  // this lane's run: block count found by the scan
+  if (inner) {
+    kb = (int64_t)fidx[fpos] / sample_run_len - run0;
+    if (!direct) {
+      // runs with keys (an empty run has no entry to find: its count is 0)
+      const bool has_keys = lane < k && min64((int64_t)lane * L, ng) < min64((int64_t)(lane + 1) * L, ng);
+      unsigned pending = __ballot_sync(0xffffffffu, has_keys) & ~(1u << (unsigned)kb);
+      const unsigned pending0 = pending;
+      int64_t q0 = fpos;
+      for (int step = 0; step < kScanChunks && pending && q0 > fbase; ++step) {
+        // skewed stretches of F (sorted runs, long ties): when the first two
+        // chunks show no other run, leave the rest to the block-sample search
+        if (step == 2 && pending == pending0) break;
+        q0 -= 32;
+        const int64_t q = q0 + lane;
+        int r = -1, bi = 0;
+        if (q >= fbase) {
+          const uint32_t si = fidx[q];
+          const uint32_t rr = si / (uint32_t)sample_run_len;
+          r = (int)((int64_t)rr - run0);
+          bi = (int)(si - rr * (uint32_t)sample_run_len);
+        }
+        // the highest lane of each run's group holds that run's latest entry
+        const unsigned same = __match_any_sync(0xffffffffu, r);
+        const bool latest = r >= 0 && r < 32 && (same >> lane) == 1u;
+        if (latest) slot[r] = bi + 1;
+        const unsigned seen = __reduce_or_sync(0xffffffffu, latest ? (1u << r) : 0u);
+        __syncwarp();
+        if (lane < k && ((seen & pending) >> lane) & 1u) scan_lo = slot[lane];
+        pending &= ~seen;
+        __syncwarp();
+      }
+      // reached the group's first sample entry: runs not seen have no block before the boundary
+      if (q0 <= fbase && lane < k && ((pending >> lane) & 1u)) scan_lo = 0;
+    }
+  }
   int64_t c = 0;
   if (lane < k) {
     const int64_t rs = min64((int64_t)lane * L, ng);
@@ -1251,12 +1301,9 @@ __global__ void __launch_bounds__(256) splitter_kernel(const KeyT* __restrict__ 
     } else if (j == jg) {
       c = len;
     } else {
-      const int64_t fpos = run0 * sample_run_len + j * G;
       const KeyT v = fkeys[fpos];
       const int64_t sidx = (int64_t)fidx[fpos];
-      const int64_t run = sidx / sample_run_len;
-      const int64_t kb = run - run0;
-      const int64_t ib = (sidx - run * sample_run_len) * sample_b;
+      const int64_t ib = (sidx - (run0 + kb) * sample_run_len) * sample_b;
       if (lane == kb) {
         c = ib;
       } else {
@@ -1273,13 +1320,18 @@ __global__ void __launch_bounds__(256) splitter_kernel(const KeyT* __restrict__ 
           }
           c = a0;
         } else {
-          // 1. blocks whose first key precedes the boundary
-          const KeyT* sr = samp + (run0 + lane) * sample_run_len;
-          const int64_t nb = (len + sample_b - 1) / sample_b;
-          int64_t lo = 0, hi = nb;
-          while (lo < hi) {
-            const int64_t mid = (lo + hi) >> 1;
-            if (precedes(sr[mid])) lo = mid + 1; else hi = mid;
+          // 1. blocks whose first key precedes the boundary (from the scan,
+          // else by binary search over the run's block sample)
+          int64_t lo = scan_lo;
+          if (lo < 0) {
+            const KeyT* sr = samp + (run0 + lane) * sample_run_len;
+            const int64_t nb = (len + sample_b - 1) / sample_b;
+            int64_t hi = nb;
+            lo = 0;
+            while (lo < hi) {
+              const int64_t mid = (lo + hi) >> 1;
+              if (precedes(sr[mid])) lo = mid + 1; else hi = mid;
+            }
           }
           // 2. inside the last such block
           if (lo == 0) {

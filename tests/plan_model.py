@@ -106,6 +106,22 @@ def model_round(keys, idx, L, geo, stats, level=0):
         kb = rr - g * k
         ib = (sidx - rr * Ls) * B
         assert np.all((kb >= 0) & (kb < k))
+        # splitter_kernel's backward scan of F's index stream: run kk's block
+        # count before boundary j is one more than the block index of run
+        # kk's last entry in F ahead of position j*G
+        fseg = fi[g * k * Ls:g * k * Ls + (ns - g * k * Ls if g == groups - 1 else k * Ls)].astype(np.int64)
+        frun = fseg // Ls - g * k
+        scan_count = {}
+        for kk in range(k):
+            pos = np.nonzero(frun == kk)[0]
+            assert np.array_equal(fseg[pos] - (g * k + kk) * Ls, np.arange(len(pos))), "a run's entries in F out of order"
+            scan_count[kk] = np.searchsorted(pos, js * G)
+            # boundaries whose scan of 256 entries would miss run kk
+            last_before = (np.where(scan_count[kk] > 0, pos[np.maximum(scan_count[kk] - 1, 0)], -1)
+                           if len(pos) else np.full(len(js), -1))
+            stats["scan_fallbacks"] = stats.get("scan_fallbacks", 0) + int(
+                np.sum((js * G - last_before > 256) & (js * G > 256) & (kk != kb)))
+            stats["scan_rows"] = stats.get("scan_rows", 0) + int(np.sum(kk != kb))
         for kk in range(k):
             rs = min(kk * L, ng)
             run = keys[gbase + rs:gbase + rs + lens[kk]]
@@ -121,6 +137,7 @@ def model_round(keys, idx, L, geo, stats, level=0):
             a0 = (m - 1) * B + 1
             a1 = np.minimum(m * B, lens[kk])
             assert np.all(np.where(m == 0, exact == 0, (a0 <= exact) & (exact <= a1)))
+            assert np.all(np.where(kk == kb, True, scan_count[kk] == m)), "scan and block-sample search disagree"
             c = np.where(kk == kb, ib, exact)
             desc[1:jg, kk] = c
             desc[jg, kk] = lens[kk]
