@@ -392,6 +392,44 @@ struct MergeCursor {
   __device__ __forceinline__ bool exhausted() const { return xa + xb == ea + eb; }
 };
 
+// Cursor of a sentinel-padded two-way merge of keys whose equal keys are
+// identical (no end checks, no side bookkeeping).  The two heads are kept
+// unordered: a step emits the smaller head, advances the cursor it came from
+// and loads that run's next key into slot 1, and moves the other cursor and
+// its key (the larger head) into slot 2.  Per step: one comparison, a
+// minimum and a maximum of the keys, two address selects, one add and the
+// load -- two instructions fewer than tracking which cursor is A and which
+// is B.  Ties take slot 1; the emitted values are those of the exact merge
+// (equal keys are interchangeable), and a cursor still advances at most once
+// per step, so it reads at most one key past the last key it took.
+template <class KeyT>
+struct MergeCursorSw {
+  uint32_t x1, x2;  // byte addresses of the two heads
+  KeyT k1, k2;      // the two heads
+
+  template <class Ld>
+  __device__ __forceinline__ void init(const Ld& ld, uint32_t a0, uint32_t b0) {
+    x1 = a0;
+    x2 = b0;
+    k1 = ld.at(a0);
+    k2 = ld.at(b0);
+  }
+
+  template <class Ld, class Cmp>
+  __device__ __forceinline__ KeyT step(const Ld& ld, Cmp cmp) {
+    constexpr uint32_t S = sizeof(KeyT);
+    const bool t = cmp(k2, k1);
+    const KeyT o = t ? k2 : k1;
+    const KeyT ko = t ? k1 : k2;
+    const uint32_t cur = t ? x2 : x1;
+    x2 = t ? x1 : x2;
+    k2 = ko;
+    x1 = cur + S;
+    k1 = ld.at(cur + S);
+    return o;
+  }
+};
+
 // One merge pair of a level: its first output position and its two runs
 // (element indices into the level's input buffer).
 struct PairRange {
@@ -478,13 +516,14 @@ __device__ __forceinline__ void merge_thread(int s, const Ld& ld, Cmp cmp, const
 //      and every window is full (a vote over `lanes`, so no divergence):
 //      then the steps run without end checks or emit predicates;
 //   2  never checked: in shared memory both runs are followed by at least
-//      ITEMS + 1 sentinel keys (the largest key under `cmp`), and all ITEMS
+//      RunPad::read sentinel keys (the largest key under `cmp`), and all ITEMS
 //      outputs are emitted, the ITEMS - m past the pair's end into the gap
 //      after it.  Merging from an exact co-rank, a window emits the m
 //      smallest remaining keys and then, both runs spent, only sentinels, so
 //      the emitted values are those of the exact merge and the spill writes
 //      sentinels into the gap.  For keys-only merges whose equal keys are
-//      identical (the output is fixed by its values).
+//      identical (the output is fixed by its values); the steps use the
+//      unordered cursor MergeCursorSw.
 template <int ITEMS, class KeyT, int NS = 2, int CHECK = 1, class Ld, class Cmp, class Emit>
 __device__ __forceinline__ void merge_window(const Ld& ld, Cmp cmp, uint32_t A0, int na, uint32_t B0, int nb, int diag,
                                              int m, unsigned lanes, const Emit& emit) {
@@ -504,10 +543,26 @@ __device__ __forceinline__ void merge_window(const Ld& ld, Cmp cmp, uint32_t A0,
     iq[q] = merge_path_in<KeyT>(ld, A0, B0, d, lo, hi, cmp);
     dq[q] = d;
   }
+  if constexpr (CHECK == 2) {
+    MergeCursorSw<KeyT> c[NS];
+#pragma unroll
+    for (int q = 0; q < NS; ++q) c[q].init(ld, A0 + (uint32_t)iq[q] * S, B0 + (uint32_t)(dq[q] - iq[q]) * S);
+#pragma unroll
+    for (int i = 0; i < H; ++i) {
+#pragma unroll
+      for (int q = 0; q < NS; ++q) {
+        if (q * H + i < ITEMS) {
+          const KeyT o = c[q].step(ld, cmp);
+          emit(q * H + i, o, 0u, true);
+        }
+      }
+    }
+    return;
+  }
   MergeCursor<KeyT> c[NS];
 #pragma unroll
   for (int q = 0; q < NS; ++q) c[q].init(ld, A0 + (uint32_t)iq[q] * S, EA, B0 + (uint32_t)(dq[q] - iq[q]) * S, EB);
-  bool unchecked = CHECK == 2;
+  bool unchecked = false;
   if constexpr (CHECK == 1) {
     bool inner = m == ITEMS;
 #pragma unroll
@@ -517,7 +572,7 @@ __device__ __forceinline__ void merge_window(const Ld& ld, Cmp cmp, uint32_t A0,
     }
     unchecked = __all_sync(lanes, inner);
   }
-  if (CHECK == 2 || unchecked) {
+  if (unchecked) {
 #pragma unroll
     for (int i = 0; i < H; ++i) {
 #pragma unroll
@@ -530,7 +585,7 @@ __device__ __forceinline__ void merge_window(const Ld& ld, Cmp cmp, uint32_t A0,
         }
       }
     }
-  } else if constexpr (CHECK != 2) {
+  } else {
 #pragma unroll
     for (int i = 0; i < H; ++i) {
 #pragma unroll

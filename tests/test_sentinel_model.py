@@ -6,7 +6,9 @@ sentinels (the largest key) and step without run-end checks.  The model
 replays a window exactly as the kernel does -- exact co-rank of each stream
 by merge path, then H unchecked steps per stream that take A on ties and load
 the key after the one taken -- and checks, on inputs full of largest keys and
-ties:
+ties, for both cursors of the kernel (MergeCursor::step_inner, which keeps A
+and B apart and takes A on ties, and MergeCursorSw, which keeps the two heads
+unordered and takes its first slot on ties):
   * the emitted values of every window equal the exact merge's at the same
     output positions (bit-exact output);
   * outputs past the pair's end (the spill into the gap) are all sentinels;
@@ -35,7 +37,7 @@ def merge_path(a, b, diag, lo, hi):
     return lo
 
 
-def window(a, b, diag, items, ns, read):
+def window(a, b, diag, items, ns, read, swap):
     na, nb = len(a), len(b)
     ap = np.concatenate([a, np.full(read, MAXK, dtype=np.uint64)])
     bp = np.concatenate([b, np.full(read, MAXK, dtype=np.uint64)])
@@ -51,6 +53,21 @@ def window(a, b, diag, items, ns, read):
     out = [None] * items
     max_over = 0
     for q in range(ns):
+        if swap:
+            # MergeCursorSw: slots (run, position) in either order
+            c1, c2 = [ap, iq[q], na], [bp, dq[q] - iq[q], nb]
+            for i in range(h):
+                pos = q * h + i
+                if pos >= items:
+                    break
+                k1, k2 = c1[0][c1[1]], c2[0][c2[1]]
+                if k2 < k1:
+                    c1, c2 = c2, c1
+                out[pos] = c1[0][c1[1]]
+                c1[1] += 1  # advance the taken cursor and load its next key
+                _ = c1[0][c1[1]]
+                max_over = max(max_over, c1[1] - c1[2] + 1)
+            continue
         xa, xb = iq[q], dq[q] - iq[q]
         ka, kb = ap[xa], bp[xb]
         for i in range(h):
@@ -71,8 +88,9 @@ def window(a, b, diag, items, ns, read):
     return out, max_over
 
 
-@pytest.mark.parametrize("items,ns", [(31, 1), (31, 2), (33, 2), (65, 1), (65, 2), (17, 2)])
-def test_sentinel_windows_match_exact_merge(items, ns):
+@pytest.mark.parametrize("swap", [False, True])
+@pytest.mark.parametrize("items,ns", [(31, 1), (31, 2), (33, 2), (65, 1), (65, 2), (17, 1), (17, 2)])
+def test_sentinel_windows_match_exact_merge(items, ns, swap):
     rng = np.random.default_rng(items * 10 + ns)
     read, gap = run_pad(items, ns)
     for trial in range(60):
@@ -92,7 +110,7 @@ def test_sentinel_windows_match_exact_merge(items, ns):
         n = na + nb
         for diag in range(0, n, items):
             m = min(items, n - diag)
-            out, over = window(a, b, diag, items, ns, read)
+            out, over = window(a, b, diag, items, ns, read, swap)
             assert over <= read, (items, ns, over, read)
             assert [int(x) for x in out[:m]] == [int(x) for x in exact[diag:diag + m]]
             assert all(int(x) == MAXK for x in out[m:])  # spill: sentinels only
@@ -100,9 +118,10 @@ def test_sentinel_windows_match_exact_merge(items, ns):
 
 
 def test_pad_sizes():
-    # the kernel instantiations: data rounds 288x31 (2 streams), 64-bit keys
-    # 256x17, base-case levels 33 keys per window
-    assert run_pad(31, 2) == (17, 30)
+    # the kernel instantiations: data rounds 288 x 31 and 256 x 17 (64-bit
+    # keys), one stream; base-case levels 65 keys per window (32-bit keys)
+    # and 33 (64-bit keys), two streams
     assert run_pad(31, 1) == (32, 32)
-    assert run_pad(17, 2) == (10, 16)
+    assert run_pad(17, 1) == (18, 18)
+    assert run_pad(65, 2) == (34, 64)
     assert run_pad(33, 2) == (18, 32)
