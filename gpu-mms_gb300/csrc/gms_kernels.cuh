@@ -120,6 +120,60 @@ __device__ __forceinline__ KeyT maybe_dec(KeyT x, int on) {
   return on ? Codec::dec(x) : x;
 }
 
+// Keys per 16-byte vector, and the position of a global key pointer within
+// its 16-byte line (in keys).  A tile whose last merge level writes its output
+// `vec_shift(g)` keys into a 16-byte-aligned shared buffer has its shared and
+// global keys 16-byte aligned at the same indices, so it can be stored with
+// 16-byte loads and stores (store_tile).
+template <class KeyT>
+struct VecKeys {
+  static constexpr int E = 16 / (int)sizeof(KeyT);
+  static constexpr bool on = sizeof(KeyT) == 4 || sizeof(KeyT) == 8;
+};
+template <class KeyT>
+__device__ __forceinline__ int vec_shift(const KeyT* g) {
+  return (int)((reinterpret_cast<uintptr_t>(g) / sizeof(KeyT)) % VecKeys<KeyT>::E);
+}
+
+// Stores the keys f[0, cnt) of shared memory to g[0, cnt) of global memory,
+// decoded when `dec`, by threads t0, t0 + nthr, ... of the CTA: 16-byte loads
+// and stores between the first and the last 16-byte boundary of g, single
+// keys at the two ends.  f must sit vec_shift(g) keys past a 16-byte boundary
+// (and g be aligned to its key size).
+template <class Codec, class KeyT>
+__device__ __forceinline__ void store_tile(const KeyT* f, KeyT* g, int cnt, int dec, int t0, int nthr) {
+  constexpr int E = VecKeys<KeyT>::E;
+  const int mis = vec_shift(g);
+  const int h = min(cnt, (E - mis) % E);  // keys before g's first 16-byte boundary
+  const int nvec = (cnt - h) / E;
+  const int tail0 = h + nvec * E;
+  const int nscal = h + (cnt - tail0);
+  for (int j = t0; j < nscal; j += nthr) {
+    const int q = j < h ? j : tail0 + (j - h);
+    g[q] = maybe_dec<Codec>(f[q], dec);
+  }
+  const uint4* fv = reinterpret_cast<const uint4*>(f + h);
+  uint4* gv = reinterpret_cast<uint4*>(g + h);
+  if (dec) {
+    for (int v = t0; v < nvec; v += nthr) {
+      uint4 w = fv[v];
+      if constexpr (sizeof(KeyT) == 4) {
+        w.x = Codec::dec(w.x);
+        w.y = Codec::dec(w.y);
+        w.z = Codec::dec(w.z);
+        w.w = Codec::dec(w.w);
+      } else {
+        const uint64_t lo = Codec::dec((uint64_t)w.x | ((uint64_t)w.y << 32));
+        const uint64_t hi = Codec::dec((uint64_t)w.z | ((uint64_t)w.w << 32));
+        w = make_uint4((uint32_t)lo, (uint32_t)(lo >> 32), (uint32_t)hi, (uint32_t)(hi >> 32));
+      }
+      gv[v] = w;
+    }
+  } else {
+    for (int v = t0; v < nvec; v += nthr) gv[v] = fv[v];
+  }
+}
+
 // Comparator on raw user bits that encodes both sides first (when `on`).
 template <class Cmp, class Codec>
 struct EncCmp {
@@ -723,8 +777,13 @@ using MergeLayoutOf =
 // of a level starts at cpre[first segment] + p*PAD), refilled with sentinels
 // at every level, so the merge steps never check run ends (merge_window CHECK
 // 2).  Without padding (payload merges, user comparators) the steps check.
+// Keys-only instantiations of at most 288 threads are compiled for three CTAs
+// per SM (the residency their shared memory allows): left to itself the
+// compiler holds the 288 x 31 merge to 40 registers and spills in the
+// vectorized tile store.
 template <class KeyT, class V, class Cmp, class Codec, int NT, int ITEMS, int NS, int COPY = 1, bool PERSIST = false>
-__global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, int64_t total_tiles) {
+__global__ void __launch_bounds__(NT, (!HasVal<V>::value && NT <= 288) ? 3 : 1)
+    merge_tiles_kernel(TileArgs<KeyT, V> a, int64_t total_tiles) {
   static_assert(!PERSIST || COPY == 1, "persistent tiles stage with bulk copies");
   pdl_wait();
   constexpr int CAP = NT * ITEMS;                        // shared-memory buffers
@@ -1066,6 +1125,11 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
     const int64_t nxt = next_tile(tau);
     Bounds nb_next;
     if (PERSIST && warp == 0 && nxt < total_tiles) nb_next = load_bounds(nxt);
+    // Keys-only sentinel-padded merges store the merged tile with 16-byte
+    // accesses: the last level writes its output vs keys into the buffer, vs
+    // being the output's position within its 16-byte line in global memory.
+    constexpr bool kVecStore = !kHasVal && PAD > 0 && VecKeys<KeyT>::on;
+    const int vs = kVecStore ? vec_shift(((d.meta[4] & GRP_ALT) ? a.out2 : a.out) + out_base) : 0;
 
     // ---- levels: window-aligned merges, pair by pair ----
     // Level 0 merges staged segment pairs (2p, 2p+1) into the merge buffer;
@@ -1090,7 +1154,9 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
         const int diag = (tid - wt[p]) * ITEMS;
         const int m = min(ITEMS, pe - ps - diag);
         const int na = pm - ps, nb = pe - pm;
-        const int yo = ps + p * PAD;  // this pair's output (PAD apart from the previous pair)
+        // this pair's output (PAD apart from the previous pair; the last
+        // level's single pair starts vs keys in)
+        const int yo = ps + p * PAD + (span >= nk ? vs : 0);
         constexpr int kCheck = PAD > 0 ? 2 : 1;
         if (lev == 0) {
           // the staged keys are encoded while read only when the round's input
@@ -1159,15 +1225,19 @@ __global__ void __launch_bounds__(NT) merge_tiles_kernel(TileArgs<KeyT, V> a, in
     const int t0 = overlap ? tid - 32 : tid;
     const int nthr = overlap ? NT - 32 : NT;
     if (t0 >= 0) {
-      const KeyT* fk = (cur ? k1 : k0);
+      const KeyT* fk = (cur ? k1 : k0) + vs;
       const V* fv = (cur ? v1 : v0);
       const int64_t tflags = d.meta[4];
       KeyT* kout = (tflags & GRP_ALT) ? a.out2 : a.out;
       V* vout = (tflags & GRP_ALT) ? a.vout2 : a.vout;
       const int dec = a.dec_on_store | ((tflags & GRP_DEC) ? 1 : 0);
-      for (int q = t0; q < cnt; q += nthr) {
-        kout[out_base + q] = maybe_dec<Codec>(fk[q], dec);
-        if constexpr (kHasVal) vout[out_base + q] = fv[q];
+      if constexpr (kVecStore) {
+        store_tile<Codec>(fk, kout + out_base, cnt, dec, t0, nthr);
+      } else {
+        for (int q = t0; q < cnt; q += nthr) {
+          kout[out_base + q] = maybe_dec<Codec>(fk[q], dec);
+          if constexpr (kHasVal) vout[out_base + q] = fv[q];
+        }
       }
       if (a.sample_out) {
         const int64_t rel0 = out_base - run_base;

@@ -110,6 +110,32 @@ def test_sort_i32_two_rounds(gms, oracle):
     assert_same(gpu_sort(gms, a), oracle.sort(a))
 
 
+# Buffers that start inside a 16-byte line: the merged tiles are stored with
+# 16-byte accesses between single keys at both ends of every tile, so output
+# (and input) pointers 1..E-1 keys past a 16-byte boundary must give the same
+# bits.  The keys around the sorted range must stay untouched.
+@pytest.mark.parametrize("dtype,shift", [(np.int32, 1), (np.int32, 3), (np.uint32, 2), (np.int64, 1),
+                                         (np.float32, 1)])
+def test_sort_unaligned_buffers(gms, oracle, dtype, shift):
+    lib = gms.load()
+    rng = np.random.default_rng(shift * 10 + np.dtype(dtype).itemsize)
+    for n in [37, 8192 + 5, 300_007, 2_000_011]:
+        if dtype == np.float32:
+            a = oracle.gen_f32(n, n)
+        else:
+            info = np.iinfo(dtype)
+            a = rng.integers(info.min, info.max, n, dtype=dtype, endpoint=True)
+        tin_all = to_dev(np.concatenate([np.zeros(shift + 2, dtype), a]))
+        tout_all = torch.full((n + shift + 2,), 7, dtype=tin_all.dtype, device="cuda")
+        tin, tout = tin_all[shift + 2:], tout_all[shift:shift + n]
+        fn = getattr(lib, "gms_sort_" + SUFFIX[np.dtype(dtype)])
+        assert fn(tin.data_ptr(), tout.data_ptr(), n, 0, stream()) == 0, lib.gms_last_error()
+        assert gms.device_status() == 0
+        got = from_dev(tout_all, dtype)
+        assert_same(got[shift:shift + n], oracle.sort(a), f"{dtype} shift={shift} n={n}")
+        assert np.all(got.view(SIGNED[got.dtype])[:shift] == 7) and np.all(got.view(SIGNED[got.dtype])[shift + n:] == 7)
+
+
 @pytest.mark.parametrize("dtype", [np.uint32, np.int64, np.uint64])
 def test_sort_integer_dtypes(gms, oracle, dtype):
     rng = np.random.default_rng(9)
