@@ -777,12 +777,19 @@ using MergeLayoutOf =
 // of a level starts at cpre[first segment] + p*PAD), refilled with sentinels
 // at every level, so the merge steps never check run ends (merge_window CHECK
 // 2).  Without padding (payload merges, user comparators) the steps check.
-// Keys-only instantiations of at most 288 threads are compiled for three CTAs
-// per SM (the residency their shared memory allows): left to itself the
-// compiler holds the 288 x 31 merge to 40 registers and spills in the
-// vectorized tile store.
+// Each instantiation is compiled for the CTAs per SM that its shared memory
+// allows (228 KB per SM, 1 KB reserved per CTA; at most 3), so its register
+// budget never lowers that residency.  Left to itself the compiler chose, for
+// the same source, 40 registers and spills for the 288 x 31 keys-only merge,
+// and 92 registers -- two CTAs per SM instead of three -- for the persistent
+// 288 x 15 float32 + int32 merge.
+template <class Lay, int NT>
+struct MergeMinBlocks {
+  static constexpr int by_smem = (int)((228u * 1024u) / (Lay::bytes + 1024u));
+  static constexpr int value = by_smem < 1 ? 1 : (by_smem > 3 ? 3 : by_smem);
+};
 template <class KeyT, class V, class Cmp, class Codec, int NT, int ITEMS, int NS, int COPY = 1, bool PERSIST = false>
-__global__ void __launch_bounds__(NT, (!HasVal<V>::value && NT <= 288) ? 3 : 1)
+__global__ void __launch_bounds__(NT, (MergeMinBlocks<MergeLayoutOf<KeyT, V, Cmp, NT, ITEMS, NS, PERSIST>, NT>::value))
     merge_tiles_kernel(TileArgs<KeyT, V> a, int64_t total_tiles) {
   static_assert(!PERSIST || COPY == 1, "persistent tiles stage with bulk copies");
   pdl_wait();
