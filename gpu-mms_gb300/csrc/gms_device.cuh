@@ -313,6 +313,22 @@ struct SmemArray {
   __device__ __forceinline__ T get(int i) const { return lds<T>(base + (uint32_t)i * (uint32_t)sizeof(T)); }
 };
 
+// Shared-memory byte address of the payload of the key at byte address `src`,
+// keys laid out from `kbase` and payloads from `vbase` at the same element
+// indices (src - kbase is a multiple of the key size): one add when key and
+// payload have the same size, a shift and an add for 8-byte keys with 4-byte
+// payloads.
+template <class KeyT, class V>
+__device__ __forceinline__ uint32_t payload_addr(uint32_t src, uint32_t kbase, uint32_t vbase) {
+  if constexpr (sizeof(KeyT) == sizeof(V)) {
+    return src + (vbase - kbase);
+  } else if constexpr (sizeof(KeyT) == 2 * sizeof(V)) {
+    return vbase + ((src - kbase) >> 1);
+  } else {
+    return vbase + (src - kbase) / (uint32_t)sizeof(KeyT) * (uint32_t)sizeof(V);
+  }
+}
+
 // Merge path over [lo, hi]: number of elements of A (byte address a0) among the
 // first `diag` outputs of the stable merge of A and B (byte address b0), A
 // winning ties, searched only inside [lo, hi].  Branch-free steps.

@@ -1170,19 +1170,33 @@ __global__ void __launch_bounds__(NT, (MergeMinBlocks<MergeLayoutOf<KeyT, V, Cmp
           // is raw caller data (a uniform branch: two specialised loops)
           auto level0 = [&](const auto& ld) {
             const uint32_t A0 = ld.addr(sbk[si]);
-            const uint32_t B0 = (si + 1 < nk) ? ld.addr(sbk[si + 1]) : A0 + (uint32_t)na * sizeof(KeyT);
+            const bool has_b = si + 1 < nk;
+            const uint32_t B0 = has_b ? ld.addr(sbk[si + 1]) : A0 + (uint32_t)na * sizeof(KeyT);
             const SmemArray<KeyT> yka(k1 + yo + diag);
             const SmemArray<V> yva(v1 + yo + diag);
-            const SmemArray<V> sva(reinterpret_cast<const V*>(stage_v));
             const int gen = a.gen_index;
+            // per run of the pair: the staged payload of the key at byte
+            // address src sits at payload_addr(src - A0 + a staged payload
+            // offset); a generated payload is the key's global index
+            uint32_t vA = 0, vB = 0, gA = 0, gB = 0;
+            if constexpr (kHasVal) {
+              const uint32_t vbase = static_cast<uint32_t>(__cvta_generic_to_shared(stage_v));
+              vA = vbase + (uint32_t)sbv[si] * (uint32_t)sizeof(V);
+              vB = has_b ? vbase + (uint32_t)sbv[si + 1] * (uint32_t)sizeof(V) : vA;
+              gA = (uint32_t)gsrc[si];
+              gB = has_b ? (uint32_t)gsrc[si + 1] : gA;
+            }
             merge_window<ITEMS, KeyT, NS, kCheck>(ld, cmp, A0, na, B0, nb, diag, m, lanes,
                                                   [&](int i, KeyT k, uint32_t src, bool ta) {
                                             yka.put(i, k);
                                             if constexpr (kHasVal) {
-                                              const int seg = ta ? si : si + 1;
-                                              const int off =
-                                                  (int)((src - ld.base) / (uint32_t)sizeof(KeyT)) - sbk[seg];
-                                              yva.put(i, gen ? (V)(gsrc[seg] + off) : sva.get(sbv[seg] + off));
+                                              const uint32_t s0 = ta ? A0 : B0;
+                                              if (gen) {
+                                                const uint32_t idx = (src - s0) / (uint32_t)sizeof(KeyT);
+                                                yva.put(i, (V)((ta ? gA : gB) + idx));
+                                              } else {
+                                                yva.put(i, lds<V>(payload_addr<KeyT, V>(src, s0, ta ? vA : vB)));
+                                              }
                                             }
                                           });
           };
@@ -1198,7 +1212,8 @@ __global__ void __launch_bounds__(NT, (MergeMinBlocks<MergeLayoutOf<KeyT, V, Cmp
           V* yv = (cur ? v0 : v1);
           const PlainLoad<KeyT> ld(xk);
           const SmemArray<KeyT> yka(yk + yo + diag);
-          const SmemArray<V> xva(xv), yva(yv + yo + diag);
+          const SmemArray<V> yva(yv + yo + diag);
+          const uint32_t xvb = static_cast<uint32_t>(__cvta_generic_to_shared(xv));
           // input runs: the outputs of pairs 2p and 2p+1 of the level below
           const uint32_t A0 = ld.addr(ps + 2 * p * PAD);
           const uint32_t B0 = mi < nk ? ld.addr(pm + (2 * p + 1) * PAD) : A0 + (uint32_t)na * sizeof(KeyT);
@@ -1206,7 +1221,7 @@ __global__ void __launch_bounds__(NT, (MergeMinBlocks<MergeLayoutOf<KeyT, V, Cmp
                                                 [&](int i, KeyT k, uint32_t src, bool) {
                                                   yka.put(i, k);
                                                   if constexpr (kHasVal)
-                                                    yva.put(i, xva.get((int)((src - ld.base) / (uint32_t)sizeof(KeyT))));
+                                                    yva.put(i, lds<V>(payload_addr<KeyT, V>(src, ld.base, xvb)));
                                                 });
         }
       }
