@@ -353,7 +353,8 @@ __global__ void __launch_bounds__(NT, (MODE == MODE_BASE && sizeof(KeyT) == 4 &&
       V* yv = (cur ? v0 : v1);
       const PlainLoad<KeyT> ld(xk);
       const SmemArray<KeyT> yka(yk + s);
-      const SmemArray<V> xva(xv), yva(yv + s);
+      const SmemArray<V> yva(yv + s);
+      const uint32_t xvb = static_cast<uint32_t>(__cvta_generic_to_shared(xv));
       const int tpp = 2 * rl / ITEMS;
       const int p = tid / tpp;
       const int diag = (tid - p * tpp) * ITEMS;
@@ -361,8 +362,7 @@ __global__ void __launch_bounds__(NT, (MODE == MODE_BASE && sizeof(KeyT) == 4 &&
       merge_window<ITEMS, KeyT, 2, 1>(ld, cmp, ld.addr(ps), rl, ld.addr(ps + rl), rl, diag, ITEMS, 0xffffffffu,
                                       [&](int i, KeyT k, uint32_t src, bool) {
                                         yka.put(i, k);
-                                        if constexpr (kHasVal)
-                                          yva.put(i, xva.get((int)((src - ld.base) / (uint32_t)sizeof(KeyT))));
+                                        if constexpr (kHasVal) yva.put(i, lds<V>(payload_addr<KeyT, V>(src, ld.base, xvb)));
                                       });
       __syncthreads();
       cur ^= 1;
@@ -451,11 +451,12 @@ __global__ void __launch_bounds__(NT, (MODE == MODE_BASE && sizeof(KeyT) == 4 &&
       if (s < cnt) {
         const PlainLoad<KeyT> ld(xk);
         const SmemArray<KeyT> yka(yk + s);
-        const SmemArray<V> xva(xv), yva(yv + s);
+        const SmemArray<V> yva(yv + s);
+        const uint32_t xvb = static_cast<uint32_t>(__cvta_generic_to_shared(xv));
         const CompactPairs pairs{pre, nk, span, (nk + span - 1) >> (31 - __clz(span))};
         merge_thread<ITEMS, KeyT>(s, ld, cmp, pairs, [&](int i, KeyT k, uint32_t src, bool, const PairRange&) {
           yka.put(i, k);
-          if constexpr (kHasVal) yva.put(i, xva.get((int)((src - ld.base) / (uint32_t)sizeof(KeyT))));
+          if constexpr (kHasVal) yva.put(i, lds<V>(payload_addr<KeyT, V>(src, ld.base, xvb)));
         });
       }
       __syncthreads();
