@@ -48,13 +48,13 @@ using KvEngine =
 // CTAs per SM the data-round merges are compiled for (their shared memory
 // decides; see MergeMinBlocks): three for keys-only and float32 + int32
 // rounds, two for uint64 + int32 rounds.
-static_assert(gms::MergeMinBlocks<gms::MergeLayoutOf<uint32_t, gms::NoVal, gms::KeyLess, 288, 31, 1, false>, 288>::value == 3,
+static_assert(gms::MergeMinBlocks<gms::MergeLayoutOf<uint32_t, gms::NoVal, gms::KeyLess, 288, 31, 1, false>>::value == 3,
               "32-bit keys-only merge: three CTAs per SM");
-static_assert(gms::MergeMinBlocks<gms::MergeLayoutOf<uint64_t, gms::NoVal, gms::KeyLess, 256, 17, 1, true>, 256>::value == 3,
+static_assert(gms::MergeMinBlocks<gms::MergeLayoutOf<uint64_t, gms::NoVal, gms::KeyLess, 256, 17, 1, true>>::value == 3,
               "64-bit keys-only merge (persistent): three CTAs per SM");
-static_assert(gms::MergeMinBlocks<gms::MergeLayoutOf<uint32_t, int32_t, gms::KeyLess, 288, 15, 1, true>, 288>::value == 3,
+static_assert(gms::MergeMinBlocks<gms::MergeLayoutOf<uint32_t, int32_t, gms::KeyLess, 288, 15, 1, true>>::value == 3,
               "32-bit key/value merge (persistent): three CTAs per SM");
-static_assert(gms::MergeMinBlocks<gms::MergeLayoutOf<uint64_t, int32_t, gms::KeyLess, 288, 15, 1, true>, 288>::value == 2,
+static_assert(gms::MergeMinBlocks<gms::MergeLayoutOf<uint64_t, int32_t, gms::KeyLess, 288, 15, 1, true>>::value == 2,
               "64-bit key/value merge (persistent): two CTAs per SM");
 
 // Fan-in of a sort of n keys over base-case runs of `base` keys: a round

@@ -784,13 +784,13 @@ using MergeLayoutOf =
 // the same source, 40 registers and spills for the 288 x 31 keys-only merge,
 // and 92 registers -- two CTAs per SM instead of three -- for the persistent
 // 288 x 15 float32 + int32 merge.
-template <class Lay, int NT>
+template <class Lay>
 struct MergeMinBlocks {
   static constexpr int by_smem = (int)((228u * 1024u) / (Lay::bytes + 1024u));
   static constexpr int value = by_smem < 1 ? 1 : (by_smem > 3 ? 3 : by_smem);
 };
 template <class KeyT, class V, class Cmp, class Codec, int NT, int ITEMS, int NS, int COPY = 1, bool PERSIST = false>
-__global__ void __launch_bounds__(NT, (MergeMinBlocks<MergeLayoutOf<KeyT, V, Cmp, NT, ITEMS, NS, PERSIST>, NT>::value))
+__global__ void __launch_bounds__(NT, (MergeMinBlocks<MergeLayoutOf<KeyT, V, Cmp, NT, ITEMS, NS, PERSIST>>::value))
     merge_tiles_kernel(TileArgs<KeyT, V> a, int64_t total_tiles) {
   static_assert(!PERSIST || COPY == 1, "persistent tiles stage with bulk copies");
   pdl_wait();
@@ -1176,9 +1176,9 @@ __global__ void __launch_bounds__(NT, (MergeMinBlocks<MergeLayoutOf<KeyT, V, Cmp
             const SmemArray<KeyT> yka(k1 + yo + diag);
             const SmemArray<V> yva(v1 + yo + diag);
             const int gen = a.gen_index;
-            // per run of the pair: the staged payload of the key at byte
-            // address src sits at payload_addr(src - A0 + a staged payload
-            // offset); a generated payload is the key's global index
+            // per run of the pair: where its staged payloads start (vA, vB:
+            // in the order of its staged keys from A0, B0) and the global
+            // index of its first key (gA, gB: generated payloads)
             uint32_t vA = 0, vB = 0, gA = 0, gB = 0;
             if constexpr (kHasVal) {
               const uint32_t vbase = static_cast<uint32_t>(__cvta_generic_to_shared(stage_v));
